@@ -1,0 +1,153 @@
+/*
+ * mpcmd — GB300-native hybrid MD / reactive multiparticle-collision engine.
+ *
+ * C ABI of the drop-in boundary.  The reference program (rober468/main
+ * collective_code/main_pattern.f95 and selkov_code/Main_SelkovDimer.f90) calls
+ * Fortran module subroutines on host arrays; this library keeps the whole
+ * state resident on one GPU and exposes one entry point per reference module
+ * call.  A Fortran driver binds these with iso_c_binding (see
+ * fortran/mpcmd_shim.f90); Python binds them with ctypes (main_gb300).
+ *
+ * Conventions: particle and cell indices are 0-based; sphere s = 2k + i for
+ * dimer k with i = 0 the catalytic (C) and i = 1 the non-catalytic (N) sphere;
+ * positions are in units of the MPC cell (a0 = 1).  Every function returns an
+ * mpcmd_status; no function aborts the process.  A context is not thread-safe
+ * and owns one CUDA stream on the current device.
+ */
+#ifndef MPCMD_H
+#define MPCMD_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mpcmd_status {
+  MPCMD_OK = 0,
+  MPCMD_ERR_CONFIG = 1,            /* invalid or unsupported configuration          */
+  MPCMD_ERR_ALLOC = 2,             /* device or host allocation failed              */
+  MPCMD_ERR_CELL_OVERFLOW = 3,     /* a cell holds more than cell_capacity of a species */
+  MPCMD_ERR_NEIGHBOUR_OVERFLOW = 4,/* shell buffers or per-particle sphere slots full */
+  MPCMD_ERR_RATTLE = 5,            /* bond constraint hit rattle_max_iter           */
+  MPCMD_ERR_INIT = 6,              /* initial placement did not converge            */
+  MPCMD_ERR_STATE = 7,             /* call out of order (e.g. step before prepare)  */
+  MPCMD_ERR_CUDA = 8,              /* a CUDA runtime call failed                    */
+  MPCMD_ERR_IO = 9,                /* checkpoint file could not be written or read  */
+  MPCMD_ERR_CHECKPOINT = 10        /* checkpoint file is corrupt or does not match  */
+} mpcmd_status;
+
+enum { MPCMD_GEOM_WALLS = 0, MPCMD_GEOM_PERIODIC = 1 };
+enum { MPCMD_KIN_NONE = 0, MPCMD_KIN_SIMPLE = 1, MPCMD_KIN_SELKOV = 2 };
+enum { MPCMD_EXCL_PARTICLE = 0, MPCMD_EXCL_CELLS = 1 };
+enum { MPCMD_CAT_DETERMINISTIC = 0, MPCMD_CAT_PROBABILISTIC = 1 };
+enum { MPCMD_PREC_FP32 = 32, MPCMD_PREC_FP64 = 64 };
+
+/* Run configuration.  The first block (through k[6]) carries the reference
+ * input decks (collective_code/input.txt read at main_pattern.f95:19-64,
+ * selkov_code/Input_SelkovDimer read at Main_SelkovDimer.f90:7-45) after the
+ * derivations of main_pattern.f95:66-127. */
+typedef struct mpcmd_config {
+  int32_t lx, ly, lz;        /* box edges in cells                                   */
+  int32_t geometry;          /* MPCMD_GEOM_*: z walls (collective) or periodic        */
+  int32_t n_dimers;          /* numdims                                             */
+  int32_t kinetics;          /* MPCMD_KIN_*: reaction_simple or Selkov RKMPC         */
+  int32_t exclusion;         /* MPCMD_EXCL_*: distribute_mod bulk rule or Affected_Cell */
+  int32_t catalysis;         /* MPCMD_CAT_*: forces_mod.f95:79-92 or ForcesMD:302-376 */
+  int32_t rotation_sense;    /* +1 mpc_rotation_mod Rodrigues, -1 RMPC projection     */
+  int32_t mpc_every;         /* MPCtstep                                             */
+  int32_t sort_every;        /* sort_step (0 = never)                                */
+  int32_t react_box_type;    /* reactive floor pattern 1..7                          */
+  int32_t react_dir;         /* 0: A->B on the floor, 1: B->A                        */
+  int32_t cell_capacity;     /* MaxA (per-cell per-species capacity, <= 255)         */
+  int32_t max_neighbour;     /* max_neighbour (per-sphere list capacity)             */
+  int32_t rattle_max_iter;   /* Con1Max / Con2Max                                    */
+  int32_t init_plane;        /* 1: mpcmd_initial places dimers in the z mid-plane    */
+  int32_t pad0;
+  int64_t n_solvent;         /* NT                                                   */
+  uint64_t seed;             /* key of the counter-based random streams              */
+  int64_t init_count[4];     /* Na0, Nb0, Ns0 (species codes 0..3) for mpcmd_initial */
+  double mass[4];            /* Ma, Mb, Ms (per species code)                        */
+  double eps_c[4];           /* EaC, EbC, EsC                                        */
+  double eps_n[4];           /* EaN, EbN, EsN                                        */
+  double rc, rn, dcn;        /* Rc, Rn, Dcn                                          */
+  double mc, mn;             /* Mc, Mn                                               */
+  double rw, ew;             /* Rw, Ew                                               */
+  double rm_delta, em;       /* Rm_delta, Em                                         */
+  double rp_ab, rp_ba;       /* RPab, RPba                                           */
+  double kT, skin, rot_angle, md_dt, mpc_dt;  /* T, skinrad, rotang, MDt, MPCt       */
+  double k[6];               /* k1 (simple) or k1..k6 (Selkov)                       */
+  /* GB300 engine options (not in the reference decks). */
+  int32_t precision;         /* MPCMD_PREC_FP32 (default) or MPCMD_PREC_FP64         */
+  int32_t shell_capacity;    /* 0 = sized from the sphere shells                     */
+  int32_t reserved[6];
+} mpcmd_config;
+
+typedef struct mpcmd_obs {
+  double momentum[3];        /* total (solvent + spheres), FP64 reduction            */
+  double solvent_momentum[3];
+  double kinetic_solvent, kinetic_dimer, potential;
+  int64_t species_count[4];
+  int64_t n_inside, n_pairs;
+  int32_t time_count, time_penetrate;
+  int64_t cstep;
+} mpcmd_obs;
+
+typedef struct mpcmd_ctx mpcmd_ctx;
+
+/* Lifetime ------------------------------------------------------------ */
+int mpcmd_create(const mpcmd_config* cfg, mpcmd_ctx** out);
+int mpcmd_destroy(mpcmd_ctx* ctx);
+const char* mpcmd_error_string(int status);
+int mpcmd_device_bytes(const mpcmd_ctx* ctx, int64_t* bytes);
+
+/* State exchange (host SoA in the reference's FP64 layout) ------------- */
+/* global_mod.f95:95-111 arrays Xsol..VZsol, flag; Xdim..FZdim as [2*nd][3]. */
+int mpcmd_upload_state(mpcmd_ctx* ctx, const double* x, const double* y, const double* z,
+                       const double* vx, const double* vy, const double* vz,
+                       const int32_t* flag, const double* dpos, const double* dvel,
+                       const double* dforce);
+int mpcmd_download_state(mpcmd_ctx* ctx, double* x, double* y, double* z,
+                         double* vx, double* vy, double* vz, int32_t* flag,
+                         double* dpos, double* dvel, double* dforce);
+/* Cell visiting order of the sort (hilbert.txt, sort_hilbert_mod.f95:57-62):
+ * order[k] = 0-based row-major id of the k-th cell.  Without it the engine
+ * uses its own Hilbert order. */
+int mpcmd_set_cell_order(mpcmd_ctx* ctx, const int32_t* order, int64_t n);
+int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count);
+
+/* Reference call surface ----------------------------------------------- */
+int mpcmd_initial(mpcmd_ctx* ctx);        /* initial_mod.f95:6-355                 */
+int mpcmd_prepare(mpcmd_ctx* ctx);        /* main_pattern.f95:168-187              */
+int mpcmd_step(mpcmd_ctx* ctx);           /* main_pattern.f95:203-225, one step    */
+int mpcmd_evolve(mpcmd_ctx* ctx);         /* evolve_mod.f95:6-732, one MD step only */
+int mpcmd_run(mpcmd_ctx* ctx, int64_t nsteps);  /* nsteps main-loop iterations     */
+int mpcmd_sort(mpcmd_ctx* ctx);           /* sort_hilbert_mod.f95:6-98             */
+int mpcmd_rebuild_lists(mpcmd_ctx* ctx);  /* neighbour_list_mod.f95:6-184          */
+int mpcmd_distribute(mpcmd_ctx* ctx);     /* distribute_mod.f95 / Affected_Cell.f90 */
+int mpcmd_mpc_rotation(mpcmd_ctx* ctx);   /* mpc_rotation_mod.f95 / RMPC:15-120     */
+int mpcmd_reaction(mpcmd_ctx* ctx);       /* reaction_mod.f95:8-66 / RMPC:127-324   */
+int mpcmd_observables(mpcmd_ctx* ctx, mpcmd_obs* out);  /* output_mod.f95:681-806   */
+int mpcmd_checkpoint(mpcmd_ctx* ctx, const char* path); /* restart_mod.f95 state    */
+int mpcmd_restore(mpcmd_ctx* ctx, const char* path);
+
+/* Inspection (parity tests) -------------------------------------------- */
+int mpcmd_get_new_cell(mpcmd_ctx* ctx, int64_t* newcell);           /* NewCellN     */
+int mpcmd_get_cell_rotation(mpcmd_ctx* ctx, double* cm, double* axis, int32_t* count);
+int mpcmd_get_distribute(mpcmd_ctx* ctx, int32_t* counts, int64_t* first);
+int mpcmd_get_affected(mpcmd_ctx* ctx, int32_t* affected);
+int mpcmd_get_shift(mpcmd_ctx* ctx, double* shift);
+int mpcmd_get_pairs(mpcmd_ctx* ctx, int64_t* n_pairs, int64_t* particle, int32_t* sphere);
+int mpcmd_get_inside(mpcmd_ctx* ctx, int64_t* n_inside, int64_t* idx);
+int mpcmd_get_counters(mpcmd_ctx* ctx, int64_t* counters, int32_t n);
+int mpcmd_reactive_grid_table(mpcmd_ctx* ctx, int32_t* table);
+int mpcmd_cell_order(mpcmd_ctx* ctx, int32_t* order);
+int64_t mpcmd_kernel_launches(mpcmd_ctx* ctx);
+
+/* Contract random numbers (same streams as the engine), for checkers. */
+double mpcmd_contract_u01(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
+                          uint32_t step, int which);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,304 @@
+"""GB300-native hybrid MD / reactive multiparticle-collision engine.
+
+Python front end of the C ABI in include/mpcmd.h (libmpcmd.so, built in-tree
+by main_gb300/build.py).  ``Engine`` mirrors the reference module call
+surface of rober468/main (collective_code/main_pattern.f95 and the modules it
+calls): ``initial``, ``prepare``, ``evolve``, ``distribute``, ``mpc_rotation``,
+``reaction``, ``sort``, ``rebuild_lists``, plus ``step``/``run`` for whole
+main-loop iterations.  There is no CPU fallback: every call runs the CUDA
+library, and a missing library raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import config
+from .config import MpcmdConfig, to_struct, workload  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.environ.get("MPCMD_LIB") or os.path.join(HERE, "_build", "libmpcmd.so")
+
+STATUS = {
+    0: "ok", 1: "invalid configuration", 2: "allocation failed", 3: "cell capacity exceeded",
+    4: "shell or neighbour capacity exceeded", 5: "RATTLE did not converge", 6: "initial placement failed",
+    7: "call out of order", 8: "CUDA error", 9: "checkpoint i/o failed", 10: "checkpoint corrupt or mismatched",
+}
+
+
+class MpcmdError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__("mpcmd %s failed: %s (%d)" % (what, STATUS.get(status, "?"), status))
+
+
+class MpcmdObs(C.Structure):
+    _fields_ = [
+        ("momentum", C.c_double * 3), ("solvent_momentum", C.c_double * 3), ("kinetic_solvent", C.c_double),
+        ("kinetic_dimer", C.c_double), ("potential", C.c_double), ("species_count", C.c_int64 * 4),
+        ("n_inside", C.c_int64), ("n_pairs", C.c_int64), ("time_count", C.c_int32),
+        ("time_penetrate", C.c_int32), ("cstep", C.c_int64),
+    ]
+
+
+_lib = None
+
+# Every entry point declared in include/mpcmd.h with its ctypes signature.
+_P = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+SIGNATURES = {
+    "mpcmd_create": (C.c_int, [C.POINTER(MpcmdConfig), C.POINTER(_P)]),
+    "mpcmd_destroy": (C.c_int, [_P]),
+    "mpcmd_error_string": (C.c_char_p, [C.c_int]),
+    "mpcmd_device_bytes": (C.c_int, [_P, _lp]),
+    "mpcmd_upload_state": (C.c_int, [_P, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
+    "mpcmd_download_state": (C.c_int, [_P, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
+    "mpcmd_set_cell_order": (C.c_int, [_P, _ip, C.c_int64]),
+    "mpcmd_set_step": (C.c_int, [_P, C.c_int64, C.c_int32]),
+    "mpcmd_initial": (C.c_int, [_P]),
+    "mpcmd_prepare": (C.c_int, [_P]),
+    "mpcmd_step": (C.c_int, [_P]),
+    "mpcmd_evolve": (C.c_int, [_P]),
+    "mpcmd_run": (C.c_int, [_P, C.c_int64]),
+    "mpcmd_sort": (C.c_int, [_P]),
+    "mpcmd_rebuild_lists": (C.c_int, [_P]),
+    "mpcmd_distribute": (C.c_int, [_P]),
+    "mpcmd_mpc_rotation": (C.c_int, [_P]),
+    "mpcmd_reaction": (C.c_int, [_P]),
+    "mpcmd_observables": (C.c_int, [_P, C.POINTER(MpcmdObs)]),
+    "mpcmd_checkpoint": (C.c_int, [_P, C.c_char_p]),
+    "mpcmd_restore": (C.c_int, [_P, C.c_char_p]),
+    "mpcmd_get_new_cell": (C.c_int, [_P, _lp]),
+    "mpcmd_get_cell_rotation": (C.c_int, [_P, _dp, _dp, _ip]),
+    "mpcmd_get_distribute": (C.c_int, [_P, _ip, _lp]),
+    "mpcmd_get_affected": (C.c_int, [_P, _ip]),
+    "mpcmd_get_shift": (C.c_int, [_P, _dp]),
+    "mpcmd_get_pairs": (C.c_int, [_P, _lp, _lp, _ip]),
+    "mpcmd_get_inside": (C.c_int, [_P, _lp, _lp]),
+    "mpcmd_get_counters": (C.c_int, [_P, _lp, C.c_int32]),
+    "mpcmd_reactive_grid_table": (C.c_int, [_P, _ip]),
+    "mpcmd_cell_order": (C.c_int, [_P, _ip]),
+    "mpcmd_kernel_launches": (C.c_int64, [_P]),
+    "mpcmd_contract_u01": (C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
+}
+
+
+def lib(build_if_missing=True):
+    """Load libmpcmd.so (building it if absent).  Raises if it cannot be loaded."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH) and build_if_missing:
+            from . import build as _b
+            _b.build()
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libmpcmd.so is missing; run main_gb300/build.py (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def contract_u01(seed, tag, index, extra, step, which):
+    return lib().mpcmd_contract_u01(seed, tag, index, extra, step, which)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Engine:
+    """One device-resident run (one mpcmd context on the current CUDA device)."""
+
+    def __init__(self, cfg):
+        self.cfg = dict(cfg)
+        self.struct = to_struct(self.cfg)
+        h = C.c_void_p()
+        st = lib().mpcmd_create(C.byref(self.struct), C.byref(h))
+        if st != 0:
+            raise MpcmdError(st, "create")
+        self.h = h
+        self.n = int(self.cfg["n_solvent"])
+        self.ns = 2 * int(self.cfg["n_dimers"])
+        self.ncell = int(self.cfg["lx"]) * int(self.cfg["ly"]) * int(self.cfg["lz"])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mpcmd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, st, what):
+        if st != 0:
+            raise MpcmdError(st, what)
+
+    # -- state -----------------------------------------------------------
+    def upload_state(self, st):
+        f = lambda k: np.ascontiguousarray(st[k], dtype=np.float64)
+        arrs = [f(k) for k in ("x", "y", "z", "vx", "vy", "vz")]
+        flag = np.ascontiguousarray(st["flag"], dtype=np.int32)
+        ns = max(self.ns, 1)
+        dpos = np.ascontiguousarray(st.get("dpos", np.zeros((ns, 3))), dtype=np.float64)
+        dvel = np.ascontiguousarray(st.get("dvel", np.zeros((ns, 3))), dtype=np.float64)
+        dfrc = np.ascontiguousarray(st.get("dforce", np.zeros((ns, 3))), dtype=np.float64)
+        self._keep = (arrs, flag, dpos, dvel, dfrc)
+        self._c(lib().mpcmd_upload_state(self.h, *[_ptr(a, C.c_double) for a in arrs], _ptr(flag, C.c_int32),
+                                         _ptr(dpos, C.c_double), _ptr(dvel, C.c_double), _ptr(dfrc, C.c_double)),
+                "upload_state")
+
+    def download_state(self):
+        n, ns = self.n, max(self.ns, 1)
+        out = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        out["flag"] = np.zeros(n, dtype=np.int32)
+        out["dpos"] = np.zeros((ns, 3)); out["dvel"] = np.zeros((ns, 3)); out["dforce"] = np.zeros((ns, 3))
+        self._c(lib().mpcmd_download_state(self.h, *[_ptr(out[k], C.c_double) for k in ("x", "y", "z", "vx", "vy", "vz")],
+                                           _ptr(out["flag"], C.c_int32), _ptr(out["dpos"], C.c_double),
+                                           _ptr(out["dvel"], C.c_double), _ptr(out["dforce"], C.c_double)),
+                "download_state")
+        if self.ns == 0:
+            for k in ("dpos", "dvel", "dforce"):
+                out[k] = out[k][:0]
+        return out
+
+    def set_cell_order(self, order):
+        a = np.ascontiguousarray(order, dtype=np.int32)
+        self._c(lib().mpcmd_set_cell_order(self.h, _ptr(a, C.c_int32), a.size), "set_cell_order")
+
+    def cell_order(self):
+        a = np.zeros(self.ncell, dtype=np.int32)
+        lib().mpcmd_cell_order(self.h, _ptr(a, C.c_int32))
+        return a
+
+    def set_step(self, cstep, time_count=0):
+        self._c(lib().mpcmd_set_step(self.h, cstep, time_count), "set_step")
+
+    # -- reference call surface ------------------------------------------
+    def initial(self):
+        self._c(lib().mpcmd_initial(self.h), "initial")
+
+    def prepare(self):
+        self._c(lib().mpcmd_prepare(self.h), "prepare")
+
+    def step(self):
+        self._c(lib().mpcmd_step(self.h), "step")
+
+    def evolve(self):
+        self._c(lib().mpcmd_evolve(self.h), "evolve")
+
+    def run(self, nsteps):
+        self._c(lib().mpcmd_run(self.h, nsteps), "run")
+
+    def sort(self):
+        self._c(lib().mpcmd_sort(self.h), "sort")
+
+    def rebuild_lists(self):
+        self._c(lib().mpcmd_rebuild_lists(self.h), "rebuild_lists")
+
+    def distribute(self):
+        self._c(lib().mpcmd_distribute(self.h), "distribute")
+
+    def mpc_rotation(self):
+        self._c(lib().mpcmd_mpc_rotation(self.h), "mpc_rotation")
+
+    def reaction(self):
+        self._c(lib().mpcmd_reaction(self.h), "reaction")
+
+    def checkpoint(self, path):
+        self._c(lib().mpcmd_checkpoint(self.h, path.encode()), "checkpoint")
+
+    def restore(self, path):
+        self._c(lib().mpcmd_restore(self.h, path.encode()), "restore")
+
+    def observables(self):
+        o = MpcmdObs()
+        self._c(lib().mpcmd_observables(self.h, C.byref(o)), "observables")
+        return {
+            "momentum": np.array(o.momentum[:]), "solvent_momentum": np.array(o.solvent_momentum[:]),
+            "kinetic_solvent": o.kinetic_solvent, "kinetic_dimer": o.kinetic_dimer, "potential": o.potential,
+            "species_count": np.array(o.species_count[:]), "n_inside": o.n_inside,
+            "time_count": o.time_count, "time_penetrate": o.time_penetrate, "cstep": o.cstep,
+        }
+
+    # -- inspection ------------------------------------------------------
+    def new_cell(self):
+        a = np.zeros(self.n, dtype=np.int64)
+        self._c(lib().mpcmd_get_new_cell(self.h, _ptr(a, C.c_int64)), "get_new_cell")
+        return a
+
+    def n_cells_shifted(self):
+        c = self.cfg
+        return c["lx"] * c["ly"] * (c["lz"] + 1 if c["geometry"] == config.GEOM_WALLS else c["lz"])
+
+    def cell_rotation(self):
+        nc = self.n_cells_shifted()
+        cm = np.zeros((nc, 3)); ax = np.zeros((nc, 3)); cnt = np.zeros(nc, dtype=np.int32)
+        self._c(lib().mpcmd_get_cell_rotation(self.h, _ptr(cm, C.c_double), _ptr(ax, C.c_double),
+                                              _ptr(cnt, C.c_int32)), "get_cell_rotation")
+        return cm, ax, cnt
+
+    def distribute_result(self):
+        cnt = np.zeros((self.ncell, 4), dtype=np.int32)
+        first = np.zeros((self.ncell, 4), dtype=np.int64)
+        self._c(lib().mpcmd_get_distribute(self.h, _ptr(cnt, C.c_int32), _ptr(first, C.c_int64)), "get_distribute")
+        return cnt, first
+
+    def affected(self):
+        a = np.zeros(self.ncell, dtype=np.int32)
+        self._c(lib().mpcmd_get_affected(self.h, _ptr(a, C.c_int32)), "get_affected")
+        return a
+
+    def shift(self):
+        s = np.zeros(3)
+        lib().mpcmd_get_shift(self.h, _ptr(s, C.c_double))
+        return s
+
+    def inside(self):
+        n = C.c_int64(0)
+        a = np.zeros(self.n, dtype=np.int64)
+        self._c(lib().mpcmd_get_inside(self.h, C.byref(n), _ptr(a, C.c_int64)), "get_inside")
+        return np.sort(a[: n.value])
+
+    def pairs(self):
+        """(particle, sphere) pairs of the shell lists, sorted by sphere then particle."""
+        n = C.c_int64(0)
+        cap = 8 * self.n
+        part = np.zeros(cap, dtype=np.int64)
+        sph = np.zeros(cap, dtype=np.int32)
+        self._c(lib().mpcmd_get_pairs(self.h, C.byref(n), _ptr(part, C.c_int64), _ptr(sph, C.c_int32)), "get_pairs")
+        part, sph = part[: n.value], sph[: n.value]
+        o = np.lexsort((part, sph))
+        return part[o], sph[o]
+
+    def neighbours(self, sphere):
+        part, sph = self.pairs()
+        return part[sph == sphere]
+
+    def counters(self):
+        c = np.zeros(10, dtype=np.int64)
+        self._c(lib().mpcmd_get_counters(self.h, _ptr(c, C.c_int64), 10), "get_counters")
+        keys = ("n_inside", "status", "time_penetrate", "rattle_iters", "cstep", "time_count", "abort_step",
+                "last_rebuild", "dbg_code", "dbg_val")
+        return dict(zip(keys, (int(v) for v in c)))
+
+    def reactive_grid(self):
+        t = np.zeros(int(self.cfg["lx"]) * int(self.cfg["ly"]), dtype=np.int32)
+        lib().mpcmd_reactive_grid_table(self.h, _ptr(t, C.c_int32))
+        return t
+
+    def device_bytes(self):
+        b = C.c_int64(0)
+        lib().mpcmd_device_bytes(self.h, C.byref(b))
+        return b.value
+
+
+def kernel_launches():
+    return int(lib().mpcmd_kernel_launches(None))

@@ -1,0 +1,148 @@
+// Device state of one mpcmd context and the kernel launchers the host
+// orchestration in mpcmd_engine.cu drives.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "mpcmd_device.cuh"
+
+namespace mpcmd {
+
+constexpr int TPB = 256;   // threads per block of the grid-stride kernels
+
+// Error bits accumulated on the device (mapped to mpcmd_status on the host).
+enum : int {
+  DEV_ERR_CELL_OVERFLOW = 1 << 0,
+  DEV_ERR_SHELL_OVERFLOW = 1 << 1,
+  DEV_ERR_PAIR_OVERFLOW = 1 << 2,
+  DEV_ERR_BIN_OVERFLOW = 1 << 3,
+  DEV_ERR_RATTLE = 1 << 4,
+  DEV_ERR_INIT = 1 << 5,
+};
+
+struct Counters {
+  unsigned int n_inside;          // entries of the current shell buffer
+  unsigned int n_inside_new;      // entries written by a running rebuild
+  unsigned long long maxv2;       // bits of max v^2 (double) over all particles at a rebuild
+  unsigned long long maxmsd[2];   // bits of max max_solvent_dist (double), by step parity
+  int status;                     // DEV_ERR_* bits
+  int abort_step;                 // step at which a displacement-triggered rebuild is due
+  int time_penetrate;
+  int pad;
+  unsigned long long rattle_iters;
+  double sums[16];                // observable reductions
+  int dbg_code;                   // checked builds: first failed bounds check
+  int dbg_pad;
+  long long dbg_val;
+};
+
+// Bounds check of the checked build (MPCMD_CHECKED): records the first failing
+// check and lets the caller skip the access.  Compiles to `true` otherwise.
+__device__ __forceinline__ bool chk(bool ok, Counters* c, int code, long long v) {
+#ifdef MPCMD_CHECKED
+  if (!ok && atomicCAS(&c->dbg_code, 0, code) == 0) c->dbg_val = v;
+  return ok;
+#else
+  (void)c; (void)code; (void)v;
+  return true;
+#endif
+}
+
+template <typename T>
+struct Shell {
+  uint32_t* idx;       // main index
+  uint32_t* cell;
+  T *ox, *oy, *oz, *vx, *vy, *vz;
+  T* msd;              // max_solvent_dist
+  uint8_t* flag;       // species bits | FLAG_INLIST
+  uint8_t* nonbulk;    // within the LJ cutoff of a sphere at the rebuild
+  uint8_t* np;         // number of sphere pairs
+  uint16_t* sph;       // [cap * PAIRMAX] sphere ids, ascending
+  T* pf;               // [cap * PAIRMAX * 3] pair forces kept across a step boundary
+  uint32_t* skey;      // shifted collision cell at an MPC step
+  int64_t cap;
+};
+
+template <typename T>
+struct Particles {
+  uint32_t* cell;
+  T *ox, *oy, *oz, *vx, *vy, *vz;
+  uint8_t* flag;
+};
+
+template <typename T>
+struct Dev {
+  Particles<T> p;          // main home, reference index order
+  Particles<T> p2;         // gather target of the sort
+  uint32_t* skey;          // shifted collision cell per particle (MPC steps)
+  Shell<T> sh;             // current shell buffer
+  Shell<T> sh2;            // shell buffer being built by a rebuild
+  double *dpos, *dvel, *dfrc, *dq;   // [ns*3] sphere state (FP64)
+  SphereRel<T>* srel;      // [ns] sphere positions as cell + offset
+  double* facc;            // [ns*4] -sum F_pair (xyz) and sum of pair potentials
+  double* fmot;            // [ns*4] motor-motor force and potential (j < k part)
+  double* dpot;            // [nd] potential of each dimer at the last force evaluation
+  uint32_t* bin_cnt;       // [nbins]
+  uint16_t* bin_list;      // [nbins * BIN_SLOTS]
+  void* acc;               // [ncell_shift] float4 (FP32) or double4 (FP64): n, sum v
+  T* rot;                  // [ncell_shift * 6] centre-of-mass velocity and axis
+  uint32_t* dcnt;          // [ncell] packed per-species counts (8 bits each)
+  unsigned long long* dfirst;  // [ncell * 4] first member key per species
+  uint8_t* affected;       // [ncell]
+  uint8_t* react_box;      // [lx*ly]
+  uint32_t* order_rank;    // [ncell] position of each cell in the sort order
+  uint32_t* scnt;          // [ncell] sort scratch
+  uint32_t* sstart;        // [ncell]
+  uint32_t* sfill;         // [ncell]
+  uint32_t* sidx;          // [n]
+  uint32_t* scan_tmp;      // scan scratch
+  Counters* ctr;
+  double* staging;         // host-exchange staging [n]
+  int32_t* staging_i;      // [n]
+};
+
+// Step-level launch arguments.
+struct StepArgs {
+  uint32_t step;       // cstep of the step being executed
+  int tc;              // time_count (lazy streaming factor)
+  int mpc;             // this step ends with a collision
+  int advance;         // fuse kick1 + stream of the next step
+  int rebuilt;         // a rebuild ran in this step
+  int merge_only;      // rebuild pass: lazy-stream and merge only, no lists
+  int grid;            // persistent grid size
+  double shift[3];     // collision grid shift of this step
+};
+
+template <typename T>
+struct Launch {
+  static void upload_convert(const Dev<T>& d, const KParams<T>& kp, const double* x, const double* y,
+                             const double* z, const double* vx, const double* vy, const double* vz,
+                             const int32_t* flag, cudaStream_t st);
+  static void download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, cudaStream_t st);
+  static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st);
+  static void update_srel(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
+  static void build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
+  static void rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  static void finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, double skin, cudaStream_t st);
+  static void force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  static void advance(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  static void dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode,
+                    double w3, int rattle_max, cudaStream_t st);
+  static void affected(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  static void accumulate_main(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int what, cudaStream_t st);
+  static void cells(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int what, cudaStream_t st);
+  static void rotate_main(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  static void rotate_shell(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  static void flush(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
+  static void regather(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
+  static void sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
+  static void observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, cudaStream_t st);
+  static void init_solvent(const Dev<T>& d, const KParams<T>& kp, const int64_t* bounds, double kT,
+                           const double* mass, cudaStream_t st);
+};
+
+int debug_sync(cudaStream_t st, const char* where, int line);
+void scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t st);
+int64_t scan_tmp_words(int64_t n);
+extern int64_t g_kernel_launches;
+
+}  // namespace mpcmd

@@ -1,0 +1,1348 @@
+// Kernels of the mpcmd engine.  Every kernel is templated on the working
+// precision T (float for production runs, double for the FP64 parity build)
+// and cites the reference loop it replaces.  Included once per precision by
+// mpcmd_kernels_f32.cu and mpcmd_kernels_f64.cu.
+#pragma once
+#include <cooperative_groups.h>
+#include <cstdio>
+#include "mpcmd_engine.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace mpcmd {
+
+#ifdef MPCMD_CHECKED
+#define LAUNCH_COUNT() (++g_kernel_launches, debug_sync(st, __func__, __LINE__))
+#else
+#define LAUNCH_COUNT() (++g_kernel_launches)
+#endif
+
+// ------------------------------------------------------------ helpers ----
+template <typename T>
+__device__ __forceinline__ void accum_coll(void* acc, uint32_t key, T vx, T vy, T vz);
+template <>
+__device__ __forceinline__ void accum_coll<float>(void* acc, uint32_t key, float vx, float vy, float vz) {
+  atomicAdd(reinterpret_cast<float4*>(acc) + key, make_float4(1.f, vx, vy, vz));
+}
+template <>
+__device__ __forceinline__ void accum_coll<double>(void* acc, uint32_t key, double vx, double vy, double vz) {
+  double* a = reinterpret_cast<double*>(acc) + 4 * (size_t)key;
+  atomicAdd(a + 0, 1.0);
+  atomicAdd(a + 1, vx);
+  atomicAdd(a + 2, vy);
+  atomicAdd(a + 3, vz);
+}
+
+// distribute_mod.f95:95-182: count one particle of species sp in unshifted
+// cell cid and keep the smallest ordering key (first member of the list).
+template <typename T>
+__device__ __forceinline__ void accum_dist(const Dev<T>& d, const KParams<T>& kp, uint32_t cid, int sp,
+                                           unsigned long long key) {
+  unsigned int old = atomicAdd(&d.dcnt[cid], 1u << (8 * sp));
+  unsigned int before = (old >> (8 * sp)) & 255u;
+  if (before + 1u > (unsigned)kp.cell_capacity) atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
+  atomicMin(&d.dfirst[4 * (size_t)cid + sp], key);
+}
+
+__device__ __forceinline__ unsigned long long dist_key(int group, uint32_t idx, uint32_t slot1) {
+  return ((unsigned long long)group << 63) | ((unsigned long long)idx << 31) | (unsigned long long)slot1;
+}
+
+template <typename T>
+__device__ __forceinline__ void block_max_to(unsigned long long* target, double v) {
+  __shared__ double red[TPB / 32];
+  double m = v;
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = red[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) b = fmax(b, red[i]);
+    if (b > 0) atomicMax(target, ord_bits(b));
+  }
+}
+
+// LJ 12-6 cut and shifted (forces_mod.f95:82-92).
+template <typename T>
+__device__ __forceinline__ void lj(const KParams<T>& kp, int t, T E, T dRsq, T dx, T dy, T dz,
+                                   T& fx, T& fy, T& fz, T& u) {
+  T IdRsq = (T)1 / dRsq;
+  T IdR6 = IdRsq * IdRsq * IdRsq;
+  T IdR8 = IdR6 * IdRsq;
+  T IdR12 = IdR6 * IdR6;
+  T IdR14 = IdR12 * IdRsq;
+  T Fbrack = (T)4 * (kp.r12R12[t] * IdR14 - kp.r6R6[t] * IdR8);
+  T Ubrack = (T)4 * (kp.R12[t] * IdR12 - kp.R6[t] * IdR6) + (T)1;
+  fx = E * Fbrack * dx;
+  fy = E * Fbrack * dy;
+  fz = E * Fbrack * dz;
+  u = E * Ubrack;
+}
+
+// Collision rotation of v - v_cm (mpc_rotation_mod.f95:205-228 Rodrigues form;
+// RMPC_SelkovDimer.f90:86-118 projection form).
+template <typename T>
+__device__ __forceinline__ void rotate_v(const KParams<T>& kp, const T* r, T& vx, T& vy, T& vz) {
+  const T cmx = r[0], cmy = r[1], cmz = r[2], ux = r[3], uy = r[4], uz = r[5];
+  const T c = kp.cosrot, s = kp.sinrot;
+  T dx = vx - cmx, dy = vy - cmy, dz = vz - cmz;
+  T rx, ry, rz;
+  if (kp.rotation_sense > 0) {
+    rx = dx * (c + ux * ux * ((T)1 - c)) + dy * (ux * uy * ((T)1 - c) - uz * s) + dz * (ux * uz * ((T)1 - c) + uy * s);
+    ry = dx * (ux * uy * ((T)1 - c) + uz * s) + dy * (c + uy * uy * ((T)1 - c)) + dz * (uy * uz * ((T)1 - c) - ux * s);
+    rz = dx * (ux * uz * ((T)1 - c) - uy * s) + dy * (uy * uz * ((T)1 - c) + ux * s) + dz * (c + uz * uz * ((T)1 - c));
+  } else {
+    T P = dx * ux + dy * uy + dz * uz;
+    T px = P * ux, py = P * uy, pz = P * uz;
+    T qx = dx - px, qy = dy - py, qz = dz - pz;
+    T wx = (qy * uz) - (qz * uy), wy = (qz * ux) - (qx * uz), wz = (qx * uy) - (qy * ux);
+    rx = px + qx * c + wx * s;
+    ry = py + qy * c + wy * s;
+    rz = pz + qz * c + wz * s;
+  }
+  vx = cmx + rx;
+  vy = cmy + ry;
+  vz = cmz + rz;
+}
+
+// ------------------------------------------------------- upload/download --
+template <typename T>
+__global__ void k_upload_pos(Particles<T> p, KParams<T> kp, const double* v, int comp) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    double x = v[i];
+    int L = comp == 0 ? kp.lx : (comp == 1 ? kp.ly : kp.lz);
+    double f = floor(x);
+    int c = (int)f;
+    T o = (T)(x - f);
+    if (o >= (T)1) { o -= (T)1; c += 1; }
+    if (comp < 2 || kp.geometry == 1) {
+      while (c >= L) c -= L;
+      while (c < 0) c += L;
+    } else {
+      if (c >= L) { c = L - 1; o = (T)1; }
+      if (c < 0) { c = 0; o = (T)0; }
+    }
+    uint32_t cell = comp == 0 ? 0u : p.cell[i];
+    int cx = comp == 0 ? c : cell_x(cell), cy = comp == 1 ? c : cell_y(cell), cz = comp == 2 ? c : cell_z(cell);
+    if (comp == 0) { cy = 0; cz = 0; }
+    p.cell[i] = pack_cell(cx, cy, cz);
+    (comp == 0 ? p.ox : comp == 1 ? p.oy : p.oz)[i] = o;
+  }
+}
+
+template <typename T>
+__global__ void k_upload_vel(Particles<T> p, KParams<T> kp, const double* v, int comp) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  T* dst = comp == 0 ? p.vx : comp == 1 ? p.vy : p.vz;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) dst[i] = (T)v[i];
+}
+
+template <typename T>
+__global__ void k_upload_flag(Particles<T> p, KParams<T> kp, const int32_t* f) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride)
+    p.flag[i] = (uint8_t)(f[i] & FLAG_SPECIES);
+}
+
+template <typename T>
+void Launch<T>::upload_convert(const Dev<T>& d, const KParams<T>& kp, const double* x, const double* y,
+                               const double* z, const double* vx, const double* vy, const double* vz,
+                               const int32_t* flag, cudaStream_t st) {
+  const int g = 1024;
+  const double* comps[6] = {x, y, z, vx, vy, vz};
+  for (int c = 0; c < 6; ++c) {
+    cudaMemcpyAsync(d.staging, comps[c], kp.n * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (c < 3) k_upload_pos<T><<<g, TPB, 0, st>>>(d.p, kp, d.staging, c);
+    else k_upload_vel<T><<<g, TPB, 0, st>>>(d.p, kp, d.staging, c - 3);
+    LAUNCH_COUNT();
+  }
+  cudaMemcpyAsync(d.staging_i, flag, kp.n * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+  k_upload_flag<T><<<g, TPB, 0, st>>>(d.p, kp, d.staging_i);
+  LAUNCH_COUNT();
+}
+
+template <typename T>
+__global__ void k_download(Particles<T> p, KParams<T> kp, double* out, int comp) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    uint32_t c = p.cell[i];
+    double v;
+    if (comp == 0) v = (double)cell_x(c) + (double)p.ox[i];
+    else if (comp == 1) v = (double)cell_y(c) + (double)p.oy[i];
+    else if (comp == 2) v = (double)cell_z(c) + (double)p.oz[i];
+    else v = (double)(comp == 3 ? p.vx : comp == 4 ? p.vy : p.vz)[i];
+    out[i] = v;
+  }
+}
+
+template <typename T>
+void Launch<T>::download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, cudaStream_t st) {
+  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, out, comp);
+  LAUNCH_COUNT();
+}
+
+template <typename T>
+__global__ void k_download_flag(Particles<T> p, KParams<T> kp, int32_t* out) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride)
+    out[i] = p.flag[i] & FLAG_SPECIES;
+}
+
+template <typename T>
+void Launch<T>::download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st) {
+  k_download_flag<T><<<1024, TPB, 0, st>>>(d.p, kp, out);
+  LAUNCH_COUNT();
+}
+
+// ------------------------------------------------------------- spheres ----
+template <typename T>
+__global__ void k_srel(Dev<T> d, KParams<T> kp) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= kp.ns) return;
+  SphereRel<T> r;
+  double X = d.dpos[3 * s], Y = d.dpos[3 * s + 1], Z = d.dpos[3 * s + 2];
+  double fx = floor(X), fy = floor(Y), fz = floor(Z);
+  r.cx = (int)fx; r.cy = (int)fy; r.cz = (int)fz;
+  r.ox = (T)(X - fx); r.oy = (T)(Y - fy); r.oz = (T)(Z - fz);
+  d.srel[s] = r;
+}
+
+template <typename T>
+void Launch<T>::update_srel(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
+  if (kp.ns == 0) return;
+  k_srel<T><<<(kp.ns + 127) / 128, 128, 0, st>>>(d, kp);
+  LAUNCH_COUNT();
+}
+
+// Coarse bins of BIN_EDGE^3 cells listing the spheres whose (cutoff + skin)
+// ball reaches into the bin; they replace the O(N * spheres) scan of
+// neighbour_list_mod.f95:38-57 by an O(1) candidate lookup per particle.
+// Cell range of a sphere's influence ball along one axis: [lo, hi] after
+// clamping (walls) or, when the ball spans the whole periodic axis, the full
+// axis without wrap.  Returns whether the range wraps.
+__device__ __forceinline__ bool axis_range(double X, double R, int L, bool periodic, int& lo, int& hi) {
+  lo = (int)floor(X - R);
+  hi = (int)floor(X + R);
+  if (!periodic) {
+    lo = max(lo, 0);
+    hi = min(hi, L - 1);
+    return false;
+  }
+  if (hi - lo + 1 >= L) { lo = 0; hi = L - 1; return false; }
+  return true;
+}
+
+__device__ __forceinline__ int wrap_mod(int c, int L) {
+  c %= L;
+  return c < 0 ? c + L : c;
+}
+
+// Cell c of the range [lo, hi] stands for its coarse bin when it is the first
+// cell of the range inside that bin; the only bin a wrapped range can enter
+// twice is the bin of lo.
+__device__ __forceinline__ bool bin_first(int c, int lo, int L, bool wraps, int& bin) {
+  int cc = wraps ? wrap_mod(c, L) : c;
+  bin = cc / BIN_EDGE;
+  if (c == lo) return true;
+  int pc = wraps ? wrap_mod(c - 1, L) : c - 1;
+  if (pc / BIN_EDGE == bin) return false;
+  if (wraps && wrap_mod(lo, L) / BIN_EDGE == bin) return false;
+  return true;
+}
+
+template <typename T>
+__global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= kp.ns) return;
+  const double R = (s & 1) ? Rn : Rc;
+  int lo[3], hi[3];
+  bool wr[3];
+  const int L[3] = {kp.lx, kp.ly, kp.lz};
+  const bool per[3] = {true, true, kp.geometry == 1};
+  for (int q = 0; q < 3; ++q) wr[q] = axis_range(d.dpos[3 * s + q], R, L[q], per[q], lo[q], hi[q]);
+#ifdef MPCMD_CHECKED
+  if (s < 2)
+    for (int q = 0; q < 3; ++q) { d.ctr->sums[6 * s + 2 * q] = (double)lo[q]; d.ctr->sums[6 * s + 2 * q + 1] = (double)hi[q]; }
+#endif
+  const int nbins = kp.nbx * kp.nby * kp.nbz;
+  for (int cx = lo[0]; cx <= hi[0]; ++cx) {
+    int bx;
+    if (!bin_first(cx, lo[0], L[0], wr[0], bx)) continue;
+    for (int cy = lo[1]; cy <= hi[1]; ++cy) {
+      int by;
+      if (!bin_first(cy, lo[1], L[1], wr[1], by)) continue;
+      for (int cz = lo[2]; cz <= hi[2]; ++cz) {
+        int bz;
+        if (!bin_first(cz, lo[2], L[2], wr[2], bz)) continue;
+        int bin = bx + kp.nbx * (by + kp.nby * bz);
+        if (!chk(bin >= 0 && bin < nbins, d.ctr, 108, bin)) continue;
+        unsigned int slot = atomicAdd(&d.bin_cnt[bin], 1u);
+        if (slot < (unsigned)BIN_SLOTS) d.bin_list[(size_t)bin * BIN_SLOTS + slot] = (uint16_t)s;
+        else atomicOr(&d.ctr->status, DEV_ERR_BIN_OVERFLOW);
+      }
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_bins_sort(Dev<T> d, int nbins) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  unsigned int n = min(d.bin_cnt[b], (unsigned)BIN_SLOTS);
+  uint16_t* l = d.bin_list + (size_t)b * BIN_SLOTS;
+  for (unsigned int i = 1; i < n; ++i) {
+    uint16_t v = l[i];
+    int j = (int)i - 1;
+    while (j >= 0 && l[j] > v) { l[j + 1] = l[j]; --j; }
+    l[j + 1] = v;
+  }
+  if (n < d.bin_cnt[b]) d.bin_cnt[b] = n;
+}
+
+template <typename T>
+void Launch<T>::build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
+  int nbins = kp.nbx * kp.nby * kp.nbz;
+  cudaMemsetAsync(d.bin_cnt, 0, sizeof(uint32_t) * nbins, st);
+  if (kp.ns == 0) return;
+  double Rc = sqrt((double)kp.full2[0]) + 1e-6, Rn = sqrt((double)kp.full2[1]) + 1e-6;
+  k_bins_fill<T><<<(kp.ns + 63) / 64, 64, 0, st>>>(d, kp, Rc, Rn);
+  k_bins_sort<T><<<(nbins + 255) / 256, 256, 0, st>>>(d, nbins);
+  LAUNCH_COUNT(); LAUNCH_COUNT();
+}
+
+__device__ __forceinline__ int bin_of(int lx, int ly, int nbx, int nby, uint32_t cell) {
+  return cell_x(cell) / BIN_EDGE + nbx * (cell_y(cell) / BIN_EDGE + nby * (cell_z(cell) / BIN_EDGE));
+}
+
+// ------------------------------------------------------------- rebuild ----
+// One pass over all particles at a neighbour-list rebuild
+// (evolve_mod.f95:465-564): lazy streaming of the outside particles by
+// time_count steps, merge of the shell buffer, shell membership and sphere
+// pairs for every particle (neighbour_list + inout_particle_list), max v^2 for
+// time_penetrate, and on collision steps the collision and distribute
+// accumulation of the particles that stay outside.
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_rebuild(Dev<T> d, KParams<T> kp, StepArgs a) {
+  if (d.ctr->abort_step) return;
+  const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
+  double vmax2 = 0.;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    uint8_t f = d.p.flag[i];
+    uint32_t cell;
+    T ox, oy, oz, vx, vy, vz;
+    uint8_t sp;
+    if (f & FLAG_HOME_SHELL) {
+      uint32_t j = d.p.cell[i];
+      if (!chk((int64_t)j < d.sh.cap, d.ctr, 109, j)) continue;
+      cell = d.sh.cell[j];
+      ox = d.sh.ox[j]; oy = d.sh.oy[j]; oz = d.sh.oz[j];
+      vx = d.sh.vx[j]; vy = d.sh.vy[j]; vz = d.sh.vz[j];
+      sp = d.sh.flag[j] & FLAG_SPECIES;
+    } else {
+      cell = d.p.cell[i];
+      ox = d.p.ox[i]; oy = d.p.oy[i]; oz = d.p.oz[i];
+      vx = d.p.vx[i]; vy = d.p.vy[i]; vz = d.p.vz[i];
+      sp = f & FLAG_SPECIES;
+      if (!(f & FLAG_INLIST) && a.tc > 0) {
+        uint8_t ff = sp;
+        stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, ff, true, a.tc);
+        sp = ff & FLAG_SPECIES;
+      }
+    }
+    double v2 = (double)(vx * vx + vy * vy + vz * vz);
+    vmax2 = fmax(vmax2, v2);
+    if (a.merge_only) {
+      d.p.cell[i] = cell;
+      d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
+      d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
+      d.p.flag[i] = sp;
+      continue;
+    }
+    // candidate spheres of this particle's coarse bin
+    int np = 0;
+    bool nonbulk = false;
+    uint16_t sph[PAIRMAX];
+    if (kp.ns > 0) {
+      int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
+      if (!chk(bin >= 0 && bin < kp.nbx * kp.nby * kp.nbz, d.ctr, 110, (long long)cell)) continue;
+      unsigned int nc = d.bin_cnt[bin];
+      if (!chk(nc <= (unsigned)BIN_SLOTS, d.ctr, 111, nc)) nc = 0;
+      const uint16_t* bl = d.bin_list + (size_t)bin * BIN_SLOTS;
+      for (unsigned int q = 0; q < nc; ++q) {
+        int s = bl[q];
+        if (!chk(s < kp.ns, d.ctr, 112, s)) continue;
+        SphereRel<T> sr = d.srel[s];
+        T dx, dy, dz;
+        T d2 = sep2(kp, cell, ox, oy, oz, sr, dx, dy, dz);
+        if (d2 <= kp.full2[s & 1]) {
+          if (np < PAIRMAX) sph[np] = (uint16_t)s;
+          np++;
+          if (d2 <= kp.cut2[s & 1]) nonbulk = true;
+        }
+      }
+    }
+    if (np > PAIRMAX) { atomicOr(&d.ctr->status, DEV_ERR_PAIR_OVERFLOW); np = PAIRMAX; }
+    if (np > 0) {
+      cg::coalesced_group g = cg::coalesced_threads();
+      unsigned int base = 0;
+      if (g.thread_rank() == 0) base = atomicAdd(&d.ctr->n_inside_new, g.size());
+      base = g.shfl(base, 0);
+      unsigned int j = base + g.thread_rank();
+      if ((int64_t)j >= d.sh2.cap) {
+        atomicOr(&d.ctr->status, DEV_ERR_SHELL_OVERFLOW);
+        continue;
+      }
+      d.sh2.idx[j] = (uint32_t)i;
+      d.sh2.cell[j] = cell;
+      d.sh2.ox[j] = ox; d.sh2.oy[j] = oy; d.sh2.oz[j] = oz;
+      d.sh2.vx[j] = vx; d.sh2.vy[j] = vy; d.sh2.vz[j] = vz;
+      d.sh2.msd[j] = (T)0;
+      d.sh2.flag[j] = sp | FLAG_INLIST;
+      d.sh2.nonbulk[j] = nonbulk ? 1 : 0;
+      d.sh2.np[j] = (uint8_t)np;
+      for (int q = 0; q < PAIRMAX; ++q) d.sh2.sph[(size_t)j * PAIRMAX + q] = q < np ? sph[q] : (uint16_t)0xFFFF;
+      d.p.cell[i] = j;
+      d.p.flag[i] = sp | FLAG_INLIST | FLAG_HOME_SHELL;
+    } else {
+      d.p.cell[i] = cell;
+      d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
+      d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
+      d.p.flag[i] = sp;
+      if (a.mpc) {
+        uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
+        d.skey[i] = key;
+        accum_coll<T>(d.acc, key, vx, vy, vz);
+        if (kp.kinetics != 0) accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), sp, dist_key(0, (uint32_t)i, 0));
+      }
+    }
+  }
+  block_max_to<T>(&d.ctr->maxv2, vmax2);
+}
+
+template <typename T>
+void Launch<T>::rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
+  k_rebuild<T><<<a.grid, TPB, 0, st>>>(d, kp, a);
+  LAUNCH_COUNT();
+}
+
+template <typename T>
+__global__ void k_finalize(Dev<T> d, KParams<T> kp, StepArgs a, double skin) {
+  if (d.ctr->abort_step) return;
+  double maxt = __longlong_as_double((long long)d.ctr->maxv2);
+  d.ctr->time_penetrate = (int)floor((0.5 * skin / sqrt(maxt)) / kp.dtd);
+  d.ctr->maxv2 = 0ull;
+  d.ctr->maxmsd[0] = 0ull;
+  d.ctr->maxmsd[1] = 0ull;
+  if (!a.merge_only) {
+    unsigned int m = d.ctr->n_inside_new;
+    if ((int64_t)m > d.sh2.cap) m = (unsigned int)d.sh2.cap;   // overflow is reported via status
+    d.ctr->n_inside = m;
+    d.ctr->n_inside_new = 0u;
+  }
+}
+
+template <typename T>
+void Launch<T>::finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, double skin,
+                                 cudaStream_t st) {
+  k_finalize<T><<<1, 1, 0, st>>>(d, kp, a, skin);
+  LAUNCH_COUNT();
+}
+
+// --------------------------------------------------------------- forces ----
+// Per shell particle and MD step (evolve_mod.f95:567-670 with
+// forces_mod.f95:6-140): LJ force against each sphere of its pair list in
+// sphere order with the catalytic conversion, the second half kick, and unless
+// the step ends in a collision or a call boundary the first half kick and free
+// flight of the next step (evolve_mod.f95:225-316) with its max_solvent_dist.
+// Extra blocks after the shell grid compute the sphere-sphere LJ forces
+// (forces_mod.f95:144-210) of the current sphere positions.
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs a) {
+  if (d.ctr->abort_step) return;
+  if (!a.rebuilt) {
+    double m = __longlong_as_double((long long)d.ctr->maxmsd[a.step & 1]);
+    if (m > (double)kp.msd_thr) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&d.ctr->abort_step, 0, (int)a.step);
+      return;
+    }
+  }
+  if ((int)blockIdx.x >= a.grid) {
+    // sphere-sphere forces: one warp per sphere s
+    int w = ((int)blockIdx.x - a.grid) * (TPB / 32) + (threadIdx.x >> 5);
+    int lane = threadIdx.x & 31;
+    if (w >= kp.ns) return;
+    const int s = w, ks = s >> 1, is = s & 1;
+    const SphereRel<T> rs = d.srel[s];
+    double fx = 0., fy = 0., fz = 0., pot = 0.;
+    for (int t = lane; t < kp.ns; t += 32) {
+      int kt = t >> 1, it = t & 1;
+      if (kt == ks) continue;
+      const SphereRel<T> rt = d.srel[t];
+      int type = is + it;  // 0 CC, 1 CN, 2 NN
+      float dxf = (float)(rs.cx - rt.cx) + (float)(rs.ox - rt.ox);
+      float dyf = (float)(rs.cy - rt.cy) + (float)(rs.oy - rt.oy);
+      float dzf = (float)(rs.cz - rt.cz) + (float)(rs.oz - rt.oz);
+      dxf = min_image(dxf, (float)kp.Ld[0]);
+      dyf = min_image(dyf, (float)kp.Ld[1]);
+      if (kp.geometry == 1) dzf = min_image(dzf, (float)kp.Ld[2]);
+      if (dxf * dxf + dyf * dyf + dzf * dzf > kp.mot_cut2f[type] * 1.001f + 1e-3f) continue;
+      double dx = d.dpos[3 * s] - d.dpos[3 * t], dy = d.dpos[3 * s + 1] - d.dpos[3 * t + 1];
+      double dz = d.dpos[3 * s + 2] - d.dpos[3 * t + 2];
+      dx = min_image(dx, kp.Ld[0]);
+      dy = min_image(dy, kp.Ld[1]);
+      if (kp.geometry == 1) dz = min_image(dz, kp.Ld[2]);
+      double dRsq = dx * dx + dy * dy + dz * dz;
+      if (dRsq <= kp.mot_cut2[type]) {
+        double IdRsq = 1.0 / dRsq;
+        double IdR6 = IdRsq * IdRsq * IdRsq, IdR8 = IdR6 * IdRsq, IdR12 = IdR6 * IdR6, IdR14 = IdR12 * IdRsq;
+        double Fb = 4.0 * (kp.mot_r12R12[type] * IdR14 - kp.mot_r6R6[type] * IdR8);
+        double Ub = 4.0 * (kp.mot_R12[type] * IdR12 - kp.mot_R6[type] * IdR6) + 1.0;
+        fx += kp.em * Fb * dx;
+        fy += kp.em * Fb * dy;
+        fz += kp.em * Fb * dz;
+        if (kt < ks) pot += kp.em * Ub;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      fx += __shfl_xor_sync(0xffffffffu, fx, o);
+      fy += __shfl_xor_sync(0xffffffffu, fy, o);
+      fz += __shfl_xor_sync(0xffffffffu, fz, o);
+      pot += __shfl_xor_sync(0xffffffffu, pot, o);
+    }
+    if (lane == 0) {
+      d.fmot[4 * s + 0] = fx; d.fmot[4 * s + 1] = fy; d.fmot[4 * s + 2] = fz; d.fmot[4 * s + 3] = pot;
+    }
+    return;
+  }
+  // per-block accumulation of the sphere reactions (small open-addressing table)
+  __shared__ int hid[32];
+  __shared__ T hf[32][4];
+  if (threadIdx.x < 32) { hid[threadIdx.x] = -1; hf[threadIdx.x][0] = hf[threadIdx.x][1] = hf[threadIdx.x][2] = hf[threadIdx.x][3] = (T)0; }
+  __syncthreads();
+  const unsigned int nin = d.ctr->n_inside;
+  const int64_t stride = (int64_t)a.grid * blockDim.x;
+  const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
+  double msdmax = 0.;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
+    uint32_t cell = d.sh.cell[j];
+    T ox = d.sh.ox[j], oy = d.sh.oy[j], oz = d.sh.oz[j];
+    T vx = d.sh.vx[j], vy = d.sh.vy[j], vz = d.sh.vz[j];
+    uint8_t fl = d.sh.flag[j];
+    const int np = d.sh.np[j];
+    const uint32_t idx = d.sh.idx[j];
+    T fpx[PAIRMAX], fpy[PAIRMAX], fpz[PAIRMAX];
+    uint16_t sphl[PAIRMAX];
+#pragma unroll
+    for (int q = 0; q < PAIRMAX; ++q) {
+      fpx[q] = fpy[q] = fpz[q] = (T)0;
+      sphl[q] = q < np ? d.sh.sph[(size_t)j * PAIRMAX + q] : (uint16_t)0xFFFF;
+    }
+#pragma unroll
+    for (int q = 0; q < PAIRMAX; ++q) {
+      if (q >= np) break;
+      const int s = sphl[q];
+      const int t = s & 1;
+      const SphereRel<T> sr = d.srel[s];
+      T dx, dy, dz;
+      T d2 = sep2(kp, cell, ox, oy, oz, sr, dx, dy, dz);
+      if (d2 <= kp.cut2[t]) {
+        int spc = fl & FLAG_SPECIES;
+        T E = (t == 0) ? kp.eps_c[spc] : kp.eps_n[spc];
+        if (t == 0) {
+          if (kp.catalysis == 0) {
+            if (spc == 0) { fl = (fl & ~FLAG_SPECIES) | 1; E = kp.eps_c[1]; }
+          } else if (spc == 0 || spc == 1) {
+            double u0, u1;
+            contract_pair(kp.seed, TAG_CAT, idx, (uint32_t)s, a.step, u0, u1);
+            if (spc == 0 && kp.rp_ab > u0) fl = (fl & ~FLAG_SPECIES) | 1;
+            if (spc == 1 && kp.rp_ba > u0) fl = (fl & ~FLAG_SPECIES) | 0;
+          }
+        }
+        T fx, fy, fz, u;
+        lj(kp, t, E, d2, dx, dy, dz, fx, fy, fz, u);
+        fpx[q] = fx; fpy[q] = fy; fpz[q] = fz;
+        // sphere reaction -F and potential into the block table
+        int h = s & 31;
+        bool done = false;
+        for (int probe = 0; probe < 32 && !done; ++probe) {
+          int cur = hid[h];
+          if (cur == -1) cur = atomicCAS(&hid[h], -1, s);
+          if (cur == -1 || cur == s) {
+            atomicAdd(&hf[h][0], -fx);
+            atomicAdd(&hf[h][1], -fy);
+            atomicAdd(&hf[h][2], -fz);
+            atomicAdd(&hf[h][3], u);
+            done = true;
+          } else {
+            h = (h + 1) & 31;
+          }
+        }
+        if (!done) {
+          atomicAdd(&d.facc[4 * s + 0], -(double)fx);
+          atomicAdd(&d.facc[4 * s + 1], -(double)fy);
+          atomicAdd(&d.facc[4 * s + 2], -(double)fz);
+          atomicAdd(&d.facc[4 * s + 3], (double)u);
+        }
+      }
+    }
+    const T h2 = kp.hIM[fl & FLAG_SPECIES];
+#pragma unroll
+    for (int q = 0; q < PAIRMAX; ++q) {
+      if (q >= np) break;
+      vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
+    }
+    if (a.mpc) {
+      uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
+      d.sh.skey[j] = key;
+      accum_coll<T>(d.acc, key, vx, vy, vz);
+      if (kp.kinetics != 0) {
+        bool bulk = kp.exclusion == 1 || !d.sh.nonbulk[j];
+        if (bulk)
+          accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), fl & FLAG_SPECIES,
+                     dist_key(kp.exclusion == 0 ? 1 : 0, idx, (uint32_t)j + 1u));
+      }
+    }
+    if (a.advance && !a.mpc) {
+#pragma unroll
+      for (int q = 0; q < PAIRMAX; ++q) {
+        if (q >= np) break;
+        vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
+      }
+      stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
+      T msd = d.sh.msd[j] + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
+      d.sh.msd[j] = msd;
+      msdmax = fmax(msdmax, (double)msd);
+      d.sh.cell[j] = cell;
+      d.sh.ox[j] = ox; d.sh.oy[j] = oy; d.sh.oz[j] = oz;
+    } else {
+#pragma unroll
+      for (int q = 0; q < PAIRMAX; ++q) {
+        if (q >= np) break;
+        size_t b = ((size_t)j * PAIRMAX + q) * 3;
+        d.sh.pf[b] = fpx[q]; d.sh.pf[b + 1] = fpy[q]; d.sh.pf[b + 2] = fpz[q];
+      }
+    }
+    d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
+    d.sh.flag[j] = fl;
+  }
+  if (a.advance && !a.mpc) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], msdmax);
+  __syncthreads();
+  if (threadIdx.x < 32 && hid[threadIdx.x] >= 0) {
+    int s = hid[threadIdx.x];
+    atomicAdd(&d.facc[4 * s + 0], (double)hf[threadIdx.x][0]);
+    atomicAdd(&d.facc[4 * s + 1], (double)hf[threadIdx.x][1]);
+    atomicAdd(&d.facc[4 * s + 2], (double)hf[threadIdx.x][2]);
+    atomicAdd(&d.facc[4 * s + 3], (double)hf[threadIdx.x][3]);
+  }
+}
+
+template <typename T>
+void Launch<T>::force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
+  int extra = (kp.ns + (TPB / 32) - 1) / (TPB / 32);
+  k_force<T><<<a.grid + extra, TPB, 0, st>>>(d, kp, a);
+  LAUNCH_COUNT();
+}
+
+// First half kick with the stored pair forces and free flight of the shell
+// particles (evolve_mod.f95:225-316), used after a collision step or at the
+// start of a run call; with rotate set it first applies the collision.
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, StepArgs a, int rotate) {
+  if (d.ctr->abort_step) return;
+  const unsigned int nin = d.ctr->n_inside;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  double msdmax = 0.;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
+    T vx = d.sh.vx[j], vy = d.sh.vy[j], vz = d.sh.vz[j];
+    if (rotate) {
+      uint32_t key = d.sh.skey[j];
+      rotate_v(kp, d.rot + 6 * (size_t)key, vx, vy, vz);
+    }
+    if (a.advance) {
+      uint32_t cell = d.sh.cell[j];
+      T ox = d.sh.ox[j], oy = d.sh.oy[j], oz = d.sh.oz[j];
+      uint8_t fl = d.sh.flag[j];
+      const int np = d.sh.np[j];
+      const T h2 = kp.hIM[fl & FLAG_SPECIES];
+      for (int q = 0; q < np; ++q) {
+        size_t b = ((size_t)j * PAIRMAX + q) * 3;
+        vx = vx + h2 * d.sh.pf[b]; vy = vy + h2 * d.sh.pf[b + 1]; vz = vz + h2 * d.sh.pf[b + 2];
+      }
+      stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
+      T msd = d.sh.msd[j] + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
+      d.sh.msd[j] = msd;
+      msdmax = fmax(msdmax, (double)msd);
+      d.sh.cell[j] = cell;
+      d.sh.ox[j] = ox; d.sh.oy[j] = oy; d.sh.oz[j] = oz;
+      d.sh.flag[j] = fl;
+    }
+    d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
+  }
+  if (a.advance) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], msdmax);
+}
+
+template <typename T>
+void Launch<T>::advance(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
+  k_shell_advance<T><<<a.grid, TPB, 0, st>>>(d, kp, a, 0);
+  LAUNCH_COUNT();
+}
+
+template <typename T>
+void Launch<T>::rotate_shell(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
+  k_shell_advance<T><<<a.grid, TPB, 0, st>>>(d, kp, a, 1);
+  LAUNCH_COUNT();
+}
+
+// ---------------------------------------------------------------- dimers ----
+// forces_mod.f95:273-335 as called at evolve_mod.f95:597,600 (the actual
+// arguments 3R^3 and 9R^9 bind to the dummies named r9R9 and r3R3).
+template <typename T>
+__device__ void lj_wall(const KParams<T>& kp, double zdim, double RwR, double w3, double& fz, double& pot) {
+  const double cutoff2 = (RwR * w3) * (RwR * w3);
+  const double R3 = RwR * RwR * RwR, R9 = R3 * R3 * R3;
+  const double r9R9 = 3.0 * R3, r3R3 = 9.0 * R9;
+  const double pref = 0.5 * 3. * sqrt(3.0);
+  double dR = kp.Ld[2] - zdim;
+  if (dR * dR < cutoff2) {
+    double IdRsq = 1. / (dR * dR);
+    double IdR3 = pow(IdRsq, 1.5);
+    double IdR9 = IdR3 * IdR3 * IdR3, IdR5 = IdR3 * IdRsq, IdR11 = IdR9 * IdRsq;
+    double Fb = pref * kp.ew * (r9R9 * IdR11 - r3R3 * IdR5);
+    fz = Fb * dR;
+    pot = pref * kp.ew * (R9 * IdR9 - R3 * IdR3) + 1.0;
+  }
+  dR = 0. - zdim;
+  if (dR * dR < cutoff2) {
+    double IdRsq = 1. / (dR * dR);
+    double IdR3 = pow(IdRsq, 1.5);
+    double IdR9 = IdR3 * IdR3 * IdR3, IdR5 = IdR3 * IdRsq, IdR11 = IdR9 * IdRsq;
+    double Fb = pref * kp.ew * (r9R9 * IdR11 - r3R3 * IdR5);
+    fz = fz + Fb * dR;
+    pot = pot + pref * kp.ew * (R9 * IdR9 - R3 * IdR3) + 1.0;
+  }
+}
+
+__device__ __forceinline__ double dmin_image(double d, double L) {
+  if (d > 0.5 * L) d -= L;
+  else if (d < -0.5 * L) d += L;
+  return d;
+}
+
+// One block per dimer (evolve_mod.f95:605-636 totals, :679-724 RATTLE
+// velocities, :320-417 RATTLE positions of the next step).
+// mode bit 0: finish the force step (totals + RATTLE-v); bit 1: RATTLE-x.
+template <typename T>
+__global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3, int rattle_max) {
+  if (d.ctr->abort_step) return;
+  const int k = blockIdx.x;
+  if (k >= kp.nd || threadIdx.x != 0) return;
+  const double dt = kp.dtd, Mc = kp.mc, Mn = kp.mn, Dcn = kp.dcn;
+  const double hIMc = (0.5 * dt) / Mc, hIMn = (0.5 * dt) / Mn;
+  const double IIM = 1.0 / ((1.0 / Mc) + (1.0 / Mn));
+  const bool per = kp.geometry == 1;
+  double* X1 = d.dpos + 3 * (2 * k);
+  double* X2 = d.dpos + 3 * (2 * k + 1);
+  double* V1 = d.dvel + 3 * (2 * k);
+  double* V2 = d.dvel + 3 * (2 * k + 1);
+  double* F1 = d.dfrc + 3 * (2 * k);
+  double* F2 = d.dfrc + 3 * (2 * k + 1);
+  double* Q1 = d.dq + 3 * (2 * k);
+  double* Q2 = d.dq + 3 * (2 * k + 1);
+  unsigned long long iters = 0;
+  if (mode & 1) {
+    double pot = 0.;
+    for (int i = 0; i < 2; ++i) {
+      int s = 2 * k + i;
+      double* F = d.dfrc + 3 * s;
+      double fw = 0., pw = 0.;
+      if (!per) lj_wall(kp, d.dpos[3 * s + 2], i == 0 ? kp.rwc : kp.rwn, w3, fw, pw);
+      F[0] = d.facc[4 * s + 0] + d.fmot[4 * s + 0];
+      F[1] = d.facc[4 * s + 1] + d.fmot[4 * s + 1];
+      F[2] = d.facc[4 * s + 2] + d.fmot[4 * s + 2] + fw;
+      pot += d.facc[4 * s + 3] + d.fmot[4 * s + 3] + pw;
+      d.facc[4 * s + 0] = 0.; d.facc[4 * s + 1] = 0.; d.facc[4 * s + 2] = 0.; d.facc[4 * s + 3] = 0.;
+    }
+    d.dpot[k] = pot;
+    for (int c = 0; c < 3; ++c) { V1[c] = Q1[c] + hIMc * F1[c]; V2[c] = Q2[c] + hIMn * F2[c]; }
+    int acc = 0;
+    for (;;) {
+      double dV[3], dd[3];
+      for (int c = 0; c < 3; ++c) { dV[c] = V1[c] - V2[c]; dd[c] = X1[c] - X2[c]; }
+      dd[0] = dmin_image(dd[0], kp.Ld[0]);
+      dd[1] = dmin_image(dd[1], kp.Ld[1]);
+      if (per) dd[2] = dmin_image(dd[2], kp.Ld[2]);
+      double Con2diff = 2.0 * (dV[0] * dd[0] + dV[1] * dd[1] + dV[2] * dd[2]);
+      if (fabs(Con2diff) < 1.e-8) break;
+      if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
+      for (int c = 0; c < 3; ++c) {
+        V1[c] = V1[c] + 2.0 * O * dd[c] / Mc;
+        V2[c] = V2[c] - 2.0 * O * dd[c] / Mn;
+      }
+      acc++;
+    }
+    iters += acc;
+  }
+  if (mode & 2) {
+    double pr1[3], pr2[3], dP[3];
+    for (int c = 0; c < 3; ++c) { pr1[c] = X1[c]; pr2[c] = X2[c]; dP[c] = X1[c] - X2[c]; }
+    dP[0] = dmin_image(dP[0], kp.Ld[0]);
+    dP[1] = dmin_image(dP[1], kp.Ld[1]);
+    if (per) dP[2] = dmin_image(dP[2], kp.Ld[2]);
+    for (int c = 0; c < 3; ++c) { Q1[c] = V1[c] + hIMc * F1[c]; Q2[c] = V2[c] + hIMn * F2[c]; }
+    for (int c = 0; c < 3; ++c) { X1[c] = X1[c] + dt * Q1[c]; X2[c] = X2[c] + dt * Q2[c]; }
+    for (int c = 0; c < (per ? 3 : 2); ++c) {
+      X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+      X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+    }
+    int acc = 0;
+    for (;;) {
+      double dd[3];
+      for (int c = 0; c < 3; ++c) dd[c] = X1[c] - X2[c];
+      dd[0] = dmin_image(dd[0], kp.Ld[0]);
+      dd[1] = dmin_image(dd[1], kp.Ld[1]);
+      if (per) dd[2] = dmin_image(dd[2], kp.Ld[2]);
+      double Con1diff = (dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) - Dcn * Dcn;
+      if (fabs(Con1diff) < 1.e-6) break;
+      if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      double G = -(0.25 * Con1diff * IIM / (dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2]));
+      for (int c = 0; c < 3; ++c) {
+        X1[c] = pr1[c] + Q1[c] * dt + 2.0 * G * dP[c] / Mc;
+        X2[c] = pr2[c] + Q2[c] * dt - 2.0 * G * dP[c] / Mn;
+      }
+      for (int c = 0; c < (per ? 3 : 2); ++c) {
+        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+      }
+      for (int c = 0; c < 3; ++c) {
+        Q1[c] = Q1[c] + 2.0 * G * dP[c] / (Mc * dt);
+        Q2[c] = Q2[c] - 2.0 * G * dP[c] / (Mn * dt);
+      }
+      acc++;
+    }
+    iters += acc;
+    for (int i = 0; i < 2; ++i) {
+      int s = 2 * k + i;
+      double XX = d.dpos[3 * s], YY = d.dpos[3 * s + 1], ZZ = d.dpos[3 * s + 2];
+      double fx = floor(XX), fy = floor(YY), fz = floor(ZZ);
+      SphereRel<T> r;
+      r.cx = (int)fx; r.cy = (int)fy; r.cz = (int)fz;
+      r.ox = (T)(XX - fx); r.oy = (T)(YY - fy); r.oz = (T)(ZZ - fz);
+      d.srel[s] = r;
+    }
+  }
+  if (iters) atomicAdd(&d.ctr->rattle_iters, iters);
+}
+
+template <typename T>
+void Launch<T>::dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode, double w3,
+                      int rattle_max, cudaStream_t st) {
+  if (kp.nd == 0) return;
+  k_dimer<T><<<kp.nd, 32, 0, st>>>(d, kp, a, mode, w3, rattle_max);
+  LAUNCH_COUNT();
+}
+
+// Affected_Cell.f90:22-98 for every sphere: mark the cells near a sphere so
+// the bulk reaction skips them.
+template <typename T>
+__global__ void k_affected(Dev<T> d, KParams<T> kp, double cutC, double cutN) {
+  if (d.ctr->abort_step) return;
+  const int s = blockIdx.x;
+  if (s >= kp.ns) return;
+  const double co = (s & 1) ? cutN : cutC, co2 = co * co;
+  const double X = d.dpos[3 * s], Y = d.dpos[3 * s + 1], Z = d.dpos[3 * s + 2];
+  const int lo0 = (int)ceil(X - (co + 1.0)), up0 = (int)floor(X + (co + 1.0));
+  const int lo1 = (int)ceil(Y - (co + 1.0)), up1 = (int)floor(Y + (co + 1.0));
+  const int lo2 = (int)ceil(Z - (co + 1.0)), up2 = (int)floor(Z + (co + 1.0));
+  const int n0 = up0 - lo0 + 1, n1 = up1 - lo1 + 1, n2 = up2 - lo2 + 1;
+  const int tot = n0 * n1 * n2;
+  for (int q = threadIdx.x; q < tot; q += blockDim.x) {
+    int i = lo0 + q % n0, j = lo1 + (q / n0) % n1, kk = lo2 + q / (n0 * n1);
+    double a0 = fabs((double)(float)i - X) - 1.0;
+    double b0 = fabs((double)(float)j - Y) - 1.0;
+    double c0 = fabs((double)(float)kk - Z) - 1.0;
+    if (a0 * a0 + b0 * b0 + c0 * c0 < co2) {
+      int ci = i, cj = j, ck = kk;
+      if (ci < 0) ci += kp.lx; else if (ci >= kp.lx) ci -= kp.lx;
+      if (cj < 0) cj += kp.ly; else if (cj >= kp.ly) cj -= kp.ly;
+      if (ck < 0) ck += kp.lz; else if (ck >= kp.lz) ck -= kp.lz;
+      if (ci < 0 || ci >= kp.lx || cj < 0 || cj >= kp.ly || ck < 0 || ck >= kp.lz) continue;
+      d.affected[ci + (size_t)kp.lx * (cj + (size_t)kp.ly * ck)] = 1;
+    }
+  }
+}
+
+template <typename T>
+void Launch<T>::affected(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
+  if (kp.ns == 0) return;
+  (void)a;
+  double cutC = sqrt((double)kp.cut2[0]), cutN = sqrt((double)kp.cut2[1]);
+  k_affected<T><<<kp.ns, 256, 0, st>>>(d, kp, cutC, cutN);
+  LAUNCH_COUNT();
+}
+
+// Collision / distribute accumulation over the main home (used by the
+// stand-alone mpc_rotation and distribute entry points).  what bit 0:
+// collision, bit 1: distribute.
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_accumulate_main(Dev<T> d, KParams<T> kp, StepArgs a, int what) {
+  const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    uint32_t cell = d.p.cell[i];
+    T ox = d.p.ox[i], oy = d.p.oy[i], oz = d.p.oz[i];
+    uint8_t f = d.p.flag[i];
+    if (what & 1) {
+      uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
+      d.skey[i] = key;
+      accum_coll<T>(d.acc, key, d.p.vx[i], d.p.vy[i], d.p.vz[i]);
+    }
+    if (what & 2) {
+      bool inl = (f & FLAG_INLIST) != 0;
+      bool bulk = true;
+      if (kp.exclusion == 0 && inl) {
+        int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
+        unsigned int nc = d.bin_cnt[bin];
+        const uint16_t* bl = d.bin_list + (size_t)bin * BIN_SLOTS;
+        for (unsigned int q = 0; q < nc; ++q) {
+          int s = bl[q];
+          T dx, dy, dz;
+          if (sep2(kp, cell, ox, oy, oz, d.srel[s], dx, dy, dz) <= kp.cut2[s & 1]) bulk = false;
+        }
+      }
+      if (bulk)
+        accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), f & FLAG_SPECIES,
+                   dist_key(kp.exclusion == 0 && inl ? 1 : 0, (uint32_t)i, 0));
+    }
+  }
+}
+
+template <typename T>
+void Launch<T>::accumulate_main(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int what, cudaStream_t st) {
+  k_accumulate_main<T><<<a.grid, TPB, 0, st>>>(d, kp, a, what);
+  LAUNCH_COUNT();
+}
+
+// ------------------------------------------------------------ per cell ----
+__device__ __forceinline__ void relabel_key(uint8_t* main_flag, uint8_t* shell_flag, unsigned long long key, int code) {
+  uint32_t idx = (uint32_t)((key >> 31) & 0xFFFFFFFFull);
+  uint32_t slot1 = (uint32_t)(key & 0x7FFFFFFFull);
+  if (slot1) shell_flag[slot1 - 1] = (uint8_t)((shell_flag[slot1 - 1] & ~FLAG_SPECIES) | code);
+  else main_flag[idx] = (uint8_t)((main_flag[idx] & ~FLAG_SPECIES) | code);
+}
+
+// Selkov six-channel RKMPC decision for one cell (RMPC_SelkovDimer.f90:132-321)
+// in FP64: channel 1..6 or 0.
+static __device__ int selkov_channel_fp64(const double* k, double tau, int nF, int nG, int nI, double x1, double x2) {
+  double a1 = k[0], a2 = k[1] * (double)nF, a5 = k[4] * (double)nG, a6 = k[5];
+  double a3 = (nG == 0) ? 0. : k[2] * (double)nF * (double)nG * (double)(nG - 1);
+  double a4 = (nG <= 1) ? 0. : k[3] * (double)nG * (double)(nG - 1) * (double)(nG - 2);
+  if (nI == 0) { a1 = 0.; a6 = 0.; }
+  double a00 = a1 + a2 + a3 + a4 + a5 + a6;
+  double prob = 1 - exp(-a00 * tau);
+  if (!(prob > x2)) return 0;
+  if (nI == 0 && nF == 0 && nG == 0) return 0;
+  double a0rand = a00 * x1;
+  double av[6] = {a1, a2, a3, a4, a5, a6};
+  double cum = 0.;
+  for (int c = 0; c < 6; ++c) {
+    cum = cum + av[c];
+    if (av[c] != 0. && a0rand < cum) return c + 1;
+  }
+  return 0;
+}
+
+// The same decision in FP32 with a guard band; returns -1 when any comparison
+// is too close to call in FP32 (the caller then uses the FP64 path).
+static __device__ int selkov_channel_fp32(const double* kd, float tau, int nF, int nG, int nI, double x1d, double x2d) {
+  float k0 = (float)kd[0], k1 = (float)kd[1], k2 = (float)kd[2], k3 = (float)kd[3], k4 = (float)kd[4], k5 = (float)kd[5];
+  float a1 = k0, a2 = k1 * (float)nF, a5 = k4 * (float)nG, a6 = k5;
+  float a3 = (nG == 0) ? 0.f : k2 * (float)nF * (float)nG * (float)(nG - 1);
+  float a4 = (nG <= 1) ? 0.f : k3 * (float)nG * (float)(nG - 1) * (float)(nG - 2);
+  if (nI == 0) { a1 = 0.f; a6 = 0.f; }
+  float a00 = a1 + a2 + a3 + a4 + a5 + a6;
+  float prob = 1.f - expf(-a00 * tau);
+  float x2 = (float)x2d;
+  float gap = prob - x2;
+  if (fabsf(gap) < 4e-6f) return -1;
+  if (!(gap > 0.f)) return 0;
+  if (nI == 0 && nF == 0 && nG == 0) return 0;
+  float a0rand = a00 * (float)x1d;
+  float av[6] = {a1, a2, a3, a4, a5, a6};
+  float cum = 0.f;
+  const float band = 4e-6f * a00 + 1e-30f;
+  for (int c = 0; c < 6; ++c) {
+    cum = cum + av[c];
+    if (av[c] != 0.f) {
+      if (fabsf(a0rand - cum) < band) return -1;
+      if (a0rand < cum) return c + 1;
+    }
+  }
+  return 0;
+}
+
+// One thread per cell after a collision step: centre-of-mass velocity and
+// random axis of every shifted cell (mpc_rotation_mod.f95:163-194), the bulk
+// reaction of every unshifted cell (reaction_mod.f95:41-62 or
+// RMPC_SelkovDimer.f90:127-324) and the reset of the accumulators.
+// what bit 0: collision tables, bit 1: reaction.
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs a, int what) {
+  if (d.ctr->abort_step) return;
+  const int64_t nmax = kp.ncell_shift > kp.ncell ? kp.ncell_shift : kp.ncell;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const double pi = 3.141592653589793;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nmax; c += stride) {
+    if ((what & 1) && c < kp.ncell_shift) {
+      T cmx = (T)0, cmy = (T)0, cmz = (T)0;
+      if (sizeof(T) == 4) {
+        float4* ac = reinterpret_cast<float4*>(d.acc) + c;
+        float4 v = *ac;
+        if (v.x != 0.f) {
+          if (kp.rotation_sense > 0) { cmx = (T)(v.y / v.x); cmy = (T)(v.z / v.x); cmz = (T)(v.w / v.x); }
+          else { float inv = 1.f / v.x; cmx = (T)(v.y * inv); cmy = (T)(v.z * inv); cmz = (T)(v.w * inv); }
+        }
+        *ac = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
+        double* ac = reinterpret_cast<double*>(d.acc) + 4 * (size_t)c;
+        double n = ac[0];
+        if (n != 0.) {
+          if (kp.rotation_sense > 0) { cmx = (T)(ac[1] / n); cmy = (T)(ac[2] / n); cmz = (T)(ac[3] / n); }
+          else { double inv = 1.0 / n; cmx = (T)(ac[1] * inv); cmy = (T)(ac[2] * inv); cmz = (T)(ac[3] * inv); }
+        }
+        ac[0] = ac[1] = ac[2] = ac[3] = 0.;
+      }
+      T ux, uy, uz;
+      if (sizeof(T) == 4) {
+        uint64_t m0, m1;
+        contract_bits(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, m0, m1);
+        float u1 = (float)(m0 >> 29) * (1.f / 16777216.f);
+        float u2 = (float)(m1 >> 29) * (1.f / 16777216.f);
+        float sp, cp;
+        sincospif(2.f * u1, &sp, &cp);
+        float th = 2.f * u2 - 1.f;
+        float r = sqrtf(fmaxf(1.f - th * th, 0.f));
+        ux = (T)(r * cp); uy = (T)(r * sp); uz = (T)th;
+      } else {
+        double u1, u2;
+        contract_pair(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, u1, u2);
+        double phi = 2.0 * pi * u1, theta = 2.0 * u2 - 1.0;
+        ux = (T)(sqrt(1.0 - theta * theta) * cos(phi));
+        uy = (T)(sqrt(1.0 - theta * theta) * sin(phi));
+        uz = (T)theta;
+      }
+      T* r = d.rot + 6 * (size_t)c;
+      r[0] = cmx; r[1] = cmy; r[2] = cmz; r[3] = ux; r[4] = uy; r[5] = uz;
+    }
+    if ((what & 2) && c < kp.ncell) {
+      unsigned int cnt = d.dcnt[c];
+      unsigned long long* fk = d.dfirst + 4 * (size_t)c;
+      if (kp.kinetics == 1) {
+        int nB = (cnt >> 8) & 255u;
+        double u0, u1;
+        contract_pair(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, u0, u1);
+        if (nB > 0) {
+          double a1 = kp.k[0] * (double)nB;
+          bool fire;
+          if (sizeof(T) == 4) {
+            float pf = 1.f - expf(-(float)a1 * (float)kp.tau);
+            float g = pf - (float)u0;
+            if (fabsf(g) < 4e-6f) fire = (0. < u0 && u0 <= 1.0 - exp(-a1 * kp.tau));
+            else fire = (0. < u0) && g >= 0.f;
+          } else {
+            double prob1 = 1.0 - exp(-a1 * kp.tau);
+            fire = (0. < u0 && u0 <= prob1);
+          }
+          if (fire) relabel_key(d.p.flag, d.sh.flag, fk[1], 0);
+        }
+      } else if (kp.kinetics == 2 && !d.affected[c]) {
+        const int tgt[7] = {-1, 3, 0, 0, 1, 1, 3};
+        const int code[7] = {-1, 0, 3, 1, 0, 3, 1};
+        double x1, x2;
+        contract_pair(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, x1, x2);
+        int nF = cnt & 255u, nG = (cnt >> 8) & 255u, nI = (cnt >> 24) & 255u;
+        int ch = -1;
+        if (sizeof(T) == 4) ch = selkov_channel_fp32(kp.k, (float)kp.tau, nF, nG, nI, x1, x2);
+        if (ch < 0) ch = selkov_channel_fp64(kp.k, kp.tau, nF, nG, nI, x1, x2);
+        if (ch > 0) {
+          unsigned long long key = fk[tgt[ch]];
+          if (key != ~0ull) relabel_key(d.p.flag, d.sh.flag, key, code[ch]);
+        }
+      }
+      d.dcnt[c] = 0u;
+      fk[0] = fk[1] = fk[2] = fk[3] = ~0ull;
+      d.affected[c] = 0;
+    }
+  }
+}
+
+template <typename T>
+void Launch<T>::cells(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int what, cudaStream_t st) {
+  k_cells<T><<<a.grid, TPB, 0, st>>>(d, kp, a, what);
+  LAUNCH_COUNT();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, StepArgs a) {
+  if (d.ctr->abort_step) return;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    if (d.p.flag[i] & FLAG_HOME_SHELL) continue;
+    uint32_t key = d.skey[i];
+    T vx = d.p.vx[i], vy = d.p.vy[i], vz = d.p.vz[i];
+    rotate_v(kp, d.rot + 6 * (size_t)key, vx, vy, vz);
+    d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
+  }
+}
+
+template <typename T>
+void Launch<T>::rotate_main(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
+  k_rotate_main<T><<<a.grid, TPB, 0, st>>>(d, kp, a);
+  LAUNCH_COUNT();
+}
+
+// ---------------------------------------------------- shell home moves ----
+template <typename T>
+__global__ void k_flush(Dev<T> d, KParams<T> kp) {
+  const unsigned int nin = d.ctr->n_inside;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
+    uint32_t i = d.sh.idx[j];
+    d.p.cell[i] = d.sh.cell[j];
+    d.p.ox[i] = d.sh.ox[j]; d.p.oy[i] = d.sh.oy[j]; d.p.oz[i] = d.sh.oz[j];
+    d.p.vx[i] = d.sh.vx[j]; d.p.vy[i] = d.sh.vy[j]; d.p.vz[i] = d.sh.vz[j];
+    d.p.flag[i] = (d.sh.flag[j] & FLAG_SPECIES) | FLAG_INLIST;
+  }
+}
+
+template <typename T>
+void Launch<T>::flush(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
+  k_flush<T><<<512, TPB, 0, st>>>(d, kp);
+  LAUNCH_COUNT();
+}
+
+template <typename T>
+__global__ void k_regather(Dev<T> d, KParams<T> kp) {
+  const unsigned int nin = d.ctr->n_inside;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
+    uint32_t i = d.sh.idx[j];
+    d.sh.cell[j] = d.p.cell[i];
+    d.sh.ox[j] = d.p.ox[i]; d.sh.oy[j] = d.p.oy[i]; d.sh.oz[j] = d.p.oz[i];
+    d.sh.vx[j] = d.p.vx[i]; d.sh.vy[j] = d.p.vy[i]; d.sh.vz[j] = d.p.vz[i];
+    d.sh.flag[j] = (d.p.flag[i] & FLAG_SPECIES) | FLAG_INLIST;
+    d.p.cell[i] = (uint32_t)j;
+    d.p.flag[i] = (d.p.flag[i] & FLAG_SPECIES) | FLAG_INLIST | FLAG_HOME_SHELL;
+  }
+}
+
+template <typename T>
+void Launch<T>::regather(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
+  k_regather<T><<<512, TPB, 0, st>>>(d, kp);
+  LAUNCH_COUNT();
+}
+
+// ------------------------------------------------------------------ sort ----
+// sort_hilbert_mod.f95:6-98: stable counting sort of all particles by the
+// visiting rank of their cell (bucket fill, per-cell index sort, gather).
+template <typename T>
+__global__ void k_sort_count(Dev<T> d, KParams<T> kp) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    uint32_t cid = unshifted_id(kp.lx, kp.ly, d.p.cell[i]);
+    if (!chk(cid < (uint32_t)kp.ncell, d.ctr, 101, cid)) continue;
+    uint32_t r = d.order_rank[cid];
+    if (!chk(r < (uint32_t)kp.ncell, d.ctr, 102, r)) continue;
+    atomicAdd(&d.scnt[r], 1u);
+  }
+}
+
+template <typename T>
+__global__ void k_sort_fill(Dev<T> d, KParams<T> kp) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    uint32_t cid = unshifted_id(kp.lx, kp.ly, d.p.cell[i]);
+    if (!chk(cid < (uint32_t)kp.ncell, d.ctr, 103, cid)) continue;
+    uint32_t r = d.order_rank[cid];
+    if (!chk(r < (uint32_t)kp.ncell, d.ctr, 104, r)) continue;
+    uint32_t pos = d.sstart[r] + atomicAdd(&d.sfill[r], 1u);
+    if (!chk(pos < (uint32_t)kp.n, d.ctr, 105, pos)) continue;
+    d.sidx[pos] = (uint32_t)i;
+  }
+}
+
+template <typename T>
+__global__ void k_sort_segments(Dev<T> d, KParams<T> kp) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < kp.ncell; r += stride) {
+    uint32_t b = d.sstart[r], n = d.scnt[r];
+    if (!chk((int64_t)b + n <= kp.n, d.ctr, 106, (long long)b + n)) continue;
+    uint32_t* s = d.sidx + b;
+    for (uint32_t i = 1; i < n; ++i) {
+      uint32_t v = s[i];
+      int j = (int)i - 1;
+      while (j >= 0 && s[j] > v) { s[j + 1] = s[j]; --j; }
+      s[j + 1] = v;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_sort_gather(Dev<T> d, KParams<T> kp) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < kp.n; q += stride) {
+    uint32_t i = d.sidx[q];
+    if (!chk(i < (uint32_t)kp.n, d.ctr, 107, i)) continue;
+    d.p2.cell[q] = d.p.cell[i];
+    d.p2.ox[q] = d.p.ox[i]; d.p2.oy[q] = d.p.oy[i]; d.p2.oz[q] = d.p.oz[i];
+    d.p2.vx[q] = d.p.vx[i]; d.p2.vy[q] = d.p.vy[i]; d.p2.vz[q] = d.p.vz[i];
+    d.p2.flag[q] = d.p.flag[i] & FLAG_SPECIES;
+  }
+}
+
+template <typename T>
+void Launch<T>::sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
+  cudaMemsetAsync(d.scnt, 0, sizeof(uint32_t) * kp.ncell, st);
+  cudaMemsetAsync(d.sfill, 0, sizeof(uint32_t) * kp.ncell, st);
+  k_sort_count<T><<<1024, TPB, 0, st>>>(d, kp);
+  scan_u32(d.scnt, d.sstart, kp.ncell, d.scan_tmp, st);
+  k_sort_fill<T><<<1024, TPB, 0, st>>>(d, kp);
+  k_sort_segments<T><<<1024, TPB, 0, st>>>(d, kp);
+  k_sort_gather<T><<<1024, TPB, 0, st>>>(d, kp);
+  LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT();
+  Particles<T> t = d.p; d.p = d.p2; d.p2 = t;
+}
+
+// --------------------------------------------------------------- reductions --
+template <typename T>
+__global__ void k_observables(Dev<T> d, KParams<T> kp, double m0, double m1, double m2, double m3) {
+  const double mass[4] = {m0, m1, m2, m3};
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    uint8_t f = d.p.flag[i];
+    double vx, vy, vz;
+    int sp;
+    if (f & FLAG_HOME_SHELL) {
+      uint32_t j = d.p.cell[i];
+      vx = d.sh.vx[j]; vy = d.sh.vy[j]; vz = d.sh.vz[j];
+      sp = d.sh.flag[j] & FLAG_SPECIES;
+    } else {
+      vx = d.p.vx[i]; vy = d.p.vy[i]; vz = d.p.vz[i];
+      sp = f & FLAG_SPECIES;
+    }
+    double m = mass[sp];
+    s[0] += m * vx; s[1] += m * vy; s[2] += m * vz;
+    s[3] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+    s[4 + sp] += 1.0;
+  }
+  for (int k = 0; k < 8; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&d.ctr->sums[k], v);
+  }
+}
+
+template <typename T>
+void Launch<T>::observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, cudaStream_t st) {
+  k_observables<T><<<512, TPB, 0, st>>>(d, kp, mass[0], mass[1], mass[2], mass[3]);
+  LAUNCH_COUNT();
+}
+
+// ------------------------------------------------------------------ init ----
+// initial_mod.f95:122-345 with contract draws: rejection sampling of the
+// positions against the sphere cutoffs and Box-Muller velocities (cos branch,
+// gauss_rand_mod.f95:31-39).  The mean removal runs on the host afterwards.
+template <typename T>
+__global__ void k_init_solvent(Dev<T> d, KParams<T> kp, int64_t b0, int64_t b1, int64_t b2,
+                               double v0, double v1, double v2, double v3) {
+  const double sd[4] = {v0, v1, v2, v3};
+  const double pi = 3.141592653589793;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    int code = i < b0 ? 0 : (i < b1 ? 1 : (i < b2 ? 2 : 3));
+    bool ok = false;
+    uint32_t cell = 0;
+    T ox = 0, oy = 0, oz = 0;
+    for (uint32_t at = 0; at < 1000000u && !ok; ++at) {
+      double ux, uy, uz, un;
+      contract_pair(kp.seed, TAG_INIT_POS, (uint32_t)i, at, 0, ux, uy);
+      contract_pair(kp.seed, TAG_INIT_POS, (uint32_t)i, at, 1, uz, un);
+      double X = kp.Ld[0] * ux, Y = kp.Ld[1] * uy, Z = kp.Ld[2] * uz;
+      double fx = floor(X), fy = floor(Y), fz = floor(Z);
+      int cx = min((int)fx, kp.lx - 1), cy = min((int)fy, kp.ly - 1), cz = min((int)fz, kp.lz - 1);
+      cell = pack_cell(cx, cy, cz);
+      ox = (T)(X - cx); oy = (T)(Y - cy); oz = (T)(Z - cz);
+      ok = true;
+      if (kp.ns > 0) {
+        int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
+        unsigned int nc = d.bin_cnt[bin];
+        const uint16_t* bl = d.bin_list + (size_t)bin * BIN_SLOTS;
+        for (unsigned int q = 0; q < nc && ok; ++q) {
+          int s = bl[q];
+          double dx = X - d.dpos[3 * s], dy = Y - d.dpos[3 * s + 1], dz = Z - d.dpos[3 * s + 2];
+          dx = dmin_image(dx, kp.Ld[0]);
+          dy = dmin_image(dy, kp.Ld[1]);
+          if (kp.geometry == 1) dz = dmin_image(dz, kp.Ld[2]);
+          if (dx * dx + dy * dy + dz * dz < (double)kp.cut2_strict[s & 1]) ok = false;
+        }
+      }
+    }
+    if (!ok) atomicOr(&d.ctr->status, DEV_ERR_INIT);
+    d.p.cell[i] = cell;
+    d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
+    d.p.flag[i] = (uint8_t)code;
+    T* vv[3] = {d.p.vx, d.p.vy, d.p.vz};
+    for (int comp = 0; comp < 3; ++comp) {
+      double xx, yy;
+      contract_pair(kp.seed, TAG_INIT_VEL, (uint32_t)i, (uint32_t)comp, 0, xx, yy);
+      yy = 1.0 - yy;
+      double th = 2 * pi * xx, R = sqrt(-2 * log(yy));
+      vv[comp][i] = (T)(sd[code] * (R * cos(th)) + 0.0);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_sum_vel(Dev<T> d, KParams<T> kp) {
+  double s[3] = {0, 0, 0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    s[0] += (double)d.p.vx[i]; s[1] += (double)d.p.vy[i]; s[2] += (double)d.p.vz[i];
+  }
+  for (int k = 0; k < 3; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&d.ctr->sums[8 + k], v);
+  }
+}
+
+template <typename T>
+__global__ void k_sub_mean(Dev<T> d, KParams<T> kp) {
+  const double inv = 1.0 / (double)kp.n;
+  const double mx = d.ctr->sums[8] * inv, my = d.ctr->sums[9] * inv, mz = d.ctr->sums[10] * inv;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    d.p.vx[i] = (T)((double)d.p.vx[i] - mx);
+    d.p.vy[i] = (T)((double)d.p.vy[i] - my);
+    d.p.vz[i] = (T)((double)d.p.vz[i] - mz);
+  }
+}
+
+template <typename T>
+void Launch<T>::init_solvent(const Dev<T>& d, const KParams<T>& kp, const int64_t* bounds, double kT,
+                             const double* mass, cudaStream_t st) {
+  double sd[4];
+  for (int c = 0; c < 4; ++c) sd[c] = sqrt(kT / mass[c]);
+  k_init_solvent<T><<<1024, TPB, 0, st>>>(d, kp, bounds[0], bounds[1], bounds[2], sd[0], sd[1], sd[2], sd[3]);
+  cudaMemsetAsync(&d.ctr->sums[8], 0, 3 * sizeof(double), st);
+  k_sum_vel<T><<<512, TPB, 0, st>>>(d, kp);
+  k_sub_mean<T><<<1024, TPB, 0, st>>>(d, kp);
+  LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT();
+}
+
+
+}  // namespace mpcmd
