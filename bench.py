@@ -1,0 +1,354 @@
+#!/usr/bin/env python
+"""Throughput benchmark: MPC+MD particle-steps/s on GB300.
+
+A step is one collision period: mpc_every (= 50) MD steps of the solvent and
+sphere dimers plus one reactive multiparticle collision (main_pattern.f95:
+203-225 iterated 50 times).  Particle-steps = solvent particles x MD steps, all
+50 MD steps counted for every particle.  The default workload is the 256^3-cell
+Selkov-kinetics run (167,772,160 solvent particles, 512 dimers), synthetic and
+seeded; its state (about 5 GB) is larger than L2, so no flush is needed between
+timed steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2] [--scale 1.0]
+    python bench.py --impl reference ...   (times the FP64 CPU restatement)
+
+Under torchrun each rank runs an independent replica (seed + rank); the line
+reports the aggregate over ranks with the max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MPC+MD particle-steps/s, 1 GB300; param-sweep time surrogate vs plain @≤5% err"
+UNIT = "particle-steps/s"
+WORKLOAD_TEXT = {
+    "c0": "plain single dimer: 30^3 periodic cells, 270,000 solvent, 1 dimer, reaction_simple",
+    "c1": "collective quasi-2D: 128x128x16 cells with z walls and reactive floor, 2,621,440 solvent, 64 dimers",
+    "c2": "Selkov kinetics: 256^3 periodic cells, 167,772,160 solvent (FP32 cell-relative SoA, uint8 species), "
+          "512 sphere dimers, six-channel RKMPC",
+}
+FALLBACK_HBM = 6800.0
+
+# algorithmic bytes per unit of each kernel kind (FP32 build), see the design doc
+BYTES_PER_PARTICLE_REBUILD = 46      # read flag+cell+offset+velocity (29 B), write cell+offset+flag (17 B)
+BYTES_PER_SHELL_ENTRY = 84           # shell entry written (55 B) and the previous shell entry read (29 B)
+BYTES_PER_SHELL_FORCE = 87           # shell particle read (54 B) and written back (33 B) per MD step
+BYTES_PER_PARTICLE_ROTATE = 29       # flag + shifted key + velocity read, velocity written
+BYTES_PER_CELL = 56                  # collision accumulator read + reset (32 B), rotation table written (24 B)
+BYTES_PER_CELL_REACTION = 74         # packed counts + first keys + affected, read and reset
+
+
+def rank_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rk = int(os.environ.get("RANK", "0"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rk, lr
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.path = tempfile.mktemp(prefix="mpcmd_clocks_", suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+def cpu_sample_config(name, threads):
+    from main_gb300 import config
+    # same density, dimer density and physics; a box small enough for a bounded CPU sample
+    scale = {"c0": 1.0, "c1": 0.5, "c2": 0.25}[name]
+    return config.workload(name, scale=scale, precision=64), scale
+
+
+def cpu_baseline(name, cycles_max=5, seconds=12.0):
+    """FP64 oracle (OpenMP, all host cores) on a bounded sample of the workload."""
+    from oracle.oracle import Oracle
+    import oracle.oracle as O
+    threads = os.cpu_count() or 1
+    cfg, scale = cpu_sample_config(name, threads)
+    o = Oracle(cfg, threads=threads)
+    o.initial()
+    o.prepare()
+    S = cfg["mpc_every"]
+    t0 = time.perf_counter()
+    cycles = 0
+    while cycles < cycles_max:
+        o.run(S)
+        cycles += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    value = cfg["n_solvent"] * S * cycles / dt
+    sample = ("%s scaled by %.2f per edge: %dx%dx%d cells, %d solvent, %d dimers; %d collision period(s) of %d MD "
+              "steps after prepare" % (name, scale, cfg["lx"], cfg["ly"], cfg["lz"], cfg["n_solvent"],
+                                       cfg["n_dimers"], cycles, S, ))
+    return {"value": value, "unit": UNIT, "cores": O.lib().orc_set_threads(0), "kind": "port",
+            "sample": sample, "seconds": dt}
+
+
+def pinned_state(n, ns):
+    import numpy as np
+    try:
+        import torch
+        mk = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory().numpy()
+        st = {k: mk((n,), torch.float64) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        st["flag"] = mk((n,), torch.int32)
+        for k in ("dpos", "dvel", "dforce"):
+            st[k] = mk((max(ns, 1), 3), torch.float64)
+        return st, True
+    except Exception:
+        st = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        st["flag"] = np.zeros(n, dtype=np.int32)
+        for k in ("dpos", "dvel", "dforce"):
+            st[k] = np.zeros((max(ns, 1), 3))
+        return st, False
+
+
+def gpu_arm(args, ws, rk, lr, dist):
+    import numpy as np
+    import main_gb300
+    from main_gb300 import Engine, config
+
+    main_gb300.set_device(lr)
+    extra = {"n_dimers": args.dimers} if args.dimers else {}
+    cfg = config.workload(args.workload, scale=args.scale, precision=32, seed=1 + rk, **extra)
+    S = cfg["mpc_every"]
+    N = cfg["n_solvent"]
+    e = Engine(cfg)
+    e.initial()
+    e.prepare()
+    e.run(args.warmup * S)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # pass A: headline timing (CUDA events on the engine stream)
+    barrier()
+    e.synchronize()
+    with Clocks(lr) as ck:
+        l0 = main_gb300.kernel_launches()
+        e.event_record(0)
+        e.run(args.steps * S)
+        e.event_record(1)
+        ms = e.event_elapsed(0, 1)
+        launches = main_gb300.kernel_launches() - l0
+    barrier()
+    clocks = ck.summary()
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * N * S * args.steps / (ms * 1e-3)
+
+    # pass B: per-launch timing of each kernel kind over the same kind of region
+    e.profile(True)
+    e.run(args.steps * S)
+    prof = e.profile_read()
+    e.profile(False)
+    ob = e.observables()
+    n_in = ob["n_inside"]
+    ncs = e.n_cells_shifted()
+    nc = e.ncell
+
+    def bytes_per_launch(kind):
+        if kind == "rebuild":
+            return N * BYTES_PER_PARTICLE_REBUILD + n_in * BYTES_PER_SHELL_ENTRY, N, "particles"
+        if kind == "force":
+            return n_in * BYTES_PER_SHELL_FORCE, n_in, "shell particles"
+        if kind == "rotate_main":
+            return N * BYTES_PER_PARTICLE_ROTATE, N, "particles"
+        if kind == "cells":
+            return ncs * BYTES_PER_CELL + nc * BYTES_PER_CELL_REACTION, ncs, "cells"
+        if kind == "shell_advance":
+            return n_in * BYTES_PER_SHELL_FORCE, n_in, "shell particles"
+        return None, None, None
+
+    kinds = sorted(prof, key=lambda k: -prof[k][0])
+    dom = next(k for k in kinds if bytes_per_launch(k)[0] is not None)
+    tot_ms, cnt = prof[dom]
+    avg_ms = tot_ms / max(cnt, 1)
+    b, units, unit_name = bytes_per_launch(dom)
+    peak, peak_kind = measured_hbm()
+    achieved = b / (avg_ms * 1e-3) / 1e9
+    traffic = ncu_traffic().get(args.workload, {}).get(dom)
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_kind,
+        "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+        "algorithmic_bytes_per_launch": int(b), "units_per_launch": int(units), "unit_kind": unit_name,
+        "avg_launch_ms": round(avg_ms, 4), "launches": cnt,
+        "share_of_timed": {k: round(prof[k][0] / sum(v[0] for v in prof.values()), 4) for k in kinds if prof[k][1]},
+    }
+
+    # e2e: the reference-facing C ABI with host buffers, host<->device copies inside
+    e2e = None
+    if not args.no_e2e:
+        ns = 2 * cfg["n_dimers"]
+        host, pinned = pinned_state(N, ns)
+        cur = e.download_state()
+        for k in host:
+            host[k][...] = cur[k] if k != "flag" else cur[k].astype(np.int32)
+        barrier()
+        t0 = time.perf_counter()
+        e.upload_state(host)
+        e.prepare()
+        for _ in range(args.steps):
+            e.run(S)
+            e.observables()
+        out = e.download_state()
+        t1 = time.perf_counter()
+        state_bytes = N * (6 * 8 + 4) + ns * 3 * 8 * 3
+        obs_bytes = 8 * 16 + ns * 3 * 8 + cfg["n_dimers"] * 8
+        e2e_s = t1 - t0
+        if dist is not None:
+            import torch
+            t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": ws * N * S * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(state_bytes / args.steps),
+               "d2h_bytes_per_step": int((state_bytes + args.steps * obs_bytes) / args.steps),
+               "pinned_host": pinned,
+               "what": "upload of the full host state, prepare, %d x (collision period + observables), download "
+                       "of the full host state" % args.steps}
+    return dict(value=value, ms=ms, launches=launches, clocks=clocks, roofline=roofline, e2e=e2e, cfg=cfg,
+                dev_bytes=e.device_bytes())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--dimers", type=int, default=0, help="override the dimer count (profiling cases)")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rk, lr = rank_info()
+
+    from main_gb300 import config
+    cfg0 = config.workload(args.workload, scale=args.scale, **({"n_dimers": args.dimers} if args.dimers else {}))
+    conf = {
+        "workload": WORKLOAD_TEXT[args.workload] if args.scale == 1.0 and not args.dimers else
+        "%s scaled by %.3g per edge (%dx%dx%d cells, %d solvent, %d dimers)" % (
+            args.workload, args.scale, cfg0["lx"], cfg0["ly"], cfg0["lz"], cfg0["n_solvent"], cfg0["n_dimers"]),
+        "name": args.workload, "solvent_per_rank": cfg0["n_solvent"], "dimers_per_rank": cfg0["n_dimers"],
+        "md_steps_per_step": cfg0["mpc_every"], "collisions_per_step": 1,
+        "l2": "inputs larger than L2 (resident state >> 129 MB), no flush" if cfg0["n_solvent"] > 5_000_000 else
+              "state fits in L2: every timed step streams the whole state once per collision period",
+        "parallelism": "replicas" if ws > 1 else "single",
+    }
+
+    if args.impl == "reference":
+        if rk != 0:
+            return 0
+        cb = cpu_baseline(args.workload, cycles_max=args.steps + args.warmup, seconds=1e9)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * cb["seconds"] / (args.steps + args.warmup), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": conf,
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(lr)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    r = gpu_arm(args, ws, rk, lr, dist)
+    cb = None
+    if rk == 0 and ws == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(args.workload, seconds=args.cpu_seconds)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rk == 0:
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": conf, "roofline": r["roofline"], "cpu_baseline": cb, "e2e": r["e2e"],
+                "gpu_launches": r["launches"], "clocks": r["clocks"], "device_bytes": r["dev_bytes"]}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

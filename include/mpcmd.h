@@ -143,6 +143,20 @@ int mpcmd_reactive_grid_table(mpcmd_ctx* ctx, int32_t* table);
 int mpcmd_cell_order(mpcmd_ctx* ctx, int32_t* order);
 int64_t mpcmd_kernel_launches(mpcmd_ctx* ctx);
 
+/* Measurement ---------------------------------------------------------- */
+/* Select the CUDA device of the contexts created afterwards by this thread. */
+int mpcmd_set_device(int device);
+/* Record event `slot` (0..7) on the context stream; elapsed time between two
+ * recorded slots in milliseconds (waits for the later one). */
+int mpcmd_event_record(mpcmd_ctx* ctx, int slot);
+int mpcmd_event_elapsed(mpcmd_ctx* ctx, int a, int b, double* ms);
+int mpcmd_synchronize(mpcmd_ctx* ctx);
+/* Per-launch CUDA-event timing by kernel kind: 0 rebuild, 1 force, 2 dimer,
+ * 3 cells, 4 rotate_main, 5 shell_advance, 6 bins, 7 finalize, 8 sort,
+ * 9 affected.  Enabling clears the totals. */
+int mpcmd_profile(mpcmd_ctx* ctx, int enable);
+int mpcmd_profile_read(mpcmd_ctx* ctx, double* ms, int64_t* count, int n);
+
 /* Contract random numbers (same streams as the engine), for checkers. */
 double mpcmd_contract_u01(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
                           uint32_t step, int which);

@@ -81,6 +81,12 @@ SIGNATURES = {
     "mpcmd_reactive_grid_table": (C.c_int, [_P, _ip]),
     "mpcmd_cell_order": (C.c_int, [_P, _ip]),
     "mpcmd_kernel_launches": (C.c_int64, [_P]),
+    "mpcmd_set_device": (C.c_int, [C.c_int]),
+    "mpcmd_event_record": (C.c_int, [_P, C.c_int]),
+    "mpcmd_event_elapsed": (C.c_int, [_P, C.c_int, C.c_int, _dp]),
+    "mpcmd_synchronize": (C.c_int, [_P]),
+    "mpcmd_profile": (C.c_int, [_P, C.c_int]),
+    "mpcmd_profile_read": (C.c_int, [_P, _dp, _lp, C.c_int]),
     "mpcmd_contract_u01": (C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
 }
 
@@ -294,6 +300,31 @@ class Engine:
         lib().mpcmd_reactive_grid_table(self.h, _ptr(t, C.c_int32))
         return t
 
+    # -- measurement -----------------------------------------------------
+    PROFILE_KINDS = ("rebuild", "force", "dimer", "cells", "rotate_main", "shell_advance", "bins",
+                     "finalize", "sort", "affected")
+
+    def event_record(self, slot):
+        self._c(lib().mpcmd_event_record(self.h, slot), "event_record")
+
+    def event_elapsed(self, a, b):
+        ms = C.c_double(0)
+        self._c(lib().mpcmd_event_elapsed(self.h, a, b, C.byref(ms)), "event_elapsed")
+        return ms.value
+
+    def synchronize(self):
+        self._c(lib().mpcmd_synchronize(self.h), "synchronize")
+
+    def profile(self, enable):
+        self._c(lib().mpcmd_profile(self.h, 1 if enable else 0), "profile")
+
+    def profile_read(self):
+        n = len(self.PROFILE_KINDS)
+        ms = np.zeros(n)
+        cnt = np.zeros(n, dtype=np.int64)
+        self._c(lib().mpcmd_profile_read(self.h, _ptr(ms, C.c_double), _ptr(cnt, C.c_int64), n), "profile_read")
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.PROFILE_KINDS)}
+
     def device_bytes(self):
         b = C.c_int64(0)
         lib().mpcmd_device_bytes(self.h, C.byref(b))
@@ -302,3 +333,9 @@ class Engine:
 
 def kernel_launches():
     return int(lib().mpcmd_kernel_launches(None))
+
+
+def set_device(device):
+    st = lib().mpcmd_set_device(int(device))
+    if st != 0:
+        raise MpcmdError(st, "set_device")

@@ -201,11 +201,11 @@ def workload(name, scale=1.0, **kw):
     name = name.lower()
     if name == "c0":
         L = max(8, int(round(30 * scale)))
-        cfg = base_config(lx=L, ly=L, lz=L, geometry=GEOM_PERIODIC, n_dimers=1, **kw)
+        args = dict(lx=L, ly=L, lz=L, geometry=GEOM_PERIODIC, n_dimers=1)
     elif name == "c1":
         lx = max(8, int(round(128 * scale)))
         nd = max(1, int(round(64 * scale * scale)))
-        cfg = base_config(lx=lx, ly=lx, lz=16, geometry=GEOM_WALLS, n_dimers=nd, init_plane=1, **kw)
+        args = dict(lx=lx, ly=lx, lz=16, geometry=GEOM_WALLS, n_dimers=nd, init_plane=1)
     elif name == "c2":
         L = max(8, int(round(256 * scale)))
         nd = max(1, int(round(512 * scale ** 3)))
@@ -213,17 +213,21 @@ def workload(name, scale=1.0, **kw):
         tot = sum(SELKOV_FRACTIONS)
         nf = n * SELKOV_FRACTIONS[0] // tot
         ng = n * SELKOV_FRACTIONS[1] // tot
-        counts = [nf, ng, 0, n - nf - ng]
         args = dict(lx=L, ly=L, lz=L, geometry=GEOM_PERIODIC, n_dimers=nd, kinetics=KIN_SELKOV,
                     exclusion=EXCL_CELLS, catalysis=CAT_PROBABILISTIC, rotation_sense=-1,
-                    cell_capacity=200, n_solvent=n, init_count=counts,
+                    cell_capacity=200, n_solvent=n, init_count=[nf, ng, 0, n - nf - ng],
                     eps_c=[1.0, 1.0, 0.0, 1.0], eps_n=[1.0, 0.1, 0.0, 1.0],
                     k=[1.0, 0.1, 1.0, 0.0, 0.01, 0.0], sort_every=5000)
-        args.update(kw)
-        cfg = base_config(**args)
     else:
         raise ValueError("unknown workload %r" % name)
-    return cfg
+    if "n_solvent" in kw and "init_count" not in kw and name == "c2":
+        n = kw["n_solvent"]
+        tot = sum(SELKOV_FRACTIONS)
+        nf = n * SELKOV_FRACTIONS[0] // tot
+        ng = n * SELKOV_FRACTIONS[1] // tot
+        args["init_count"] = [nf, ng, 0, n - nf - ng]
+    args.update(kw)
+    return base_config(**args)
 
 
 WORKLOAD_STEPS = {"c0": 100, "c1": 1000, "c2": 200}   # MPC steps of each workload

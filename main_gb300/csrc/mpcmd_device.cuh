@@ -143,10 +143,13 @@ __device__ __forceinline__ void renorm(T& o, int& c) {
   if (o >= (T)1) { o -= (T)1; c += 1; }
 }
 
-// Single-shift periodic wrap of a cell coordinate (evolve_mod.f95:260-264).
+// Periodic wrap of a cell coordinate.  For moves shorter than the box this is
+// the single shift of evolve_mod.f95:260-264; longer moves (which the Fortran
+// does not handle) still land inside the box, so no index leaves its table.
 __device__ __forceinline__ int wrap_cell(int c, int L) {
   if (c >= L) c -= L;
   else if (c < 0) c += L;
+  if (c >= L || c < 0) { c %= L; if (c < 0) c += L; }
   return c;
 }
 

@@ -20,6 +20,13 @@ namespace {
 
 const double kPi = 3.141592653589793;
 
+// Kernel kinds of the per-launch timing (mpcmd_profile_read order).
+enum {
+  PROF_REBUILD = 0, PROF_FORCE = 1, PROF_DIMER = 2, PROF_CELLS = 3, PROF_ROTATE_MAIN = 4,
+  PROF_SHELL_ADVANCE = 5, PROF_BINS = 6, PROF_FINALIZE = 7, PROF_SORT = 8, PROF_AFFECTED = 9,
+  PROF_KINDS = 10
+};
+
 // Hilbert index of a 3-D point (Skilling, "Programming the Hilbert curve",
 // AIP Conf. Proc. 707, 2004): axes -> transpose form, then bit interleave.
 uint64_t hilbert_index(uint32_t x, uint32_t y, uint32_t z, int bits) {
@@ -134,6 +141,11 @@ struct EngineBase {
   virtual int get_counters(int64_t* c, int32_t n) = 0;
   virtual int checkpoint(const char* path) = 0;
   virtual int restore(const char* path) = 0;
+  virtual int event_record(int slot) = 0;
+  virtual int event_elapsed(int a, int b, double* ms) = 0;
+  virtual int synchronize() = 0;
+  virtual int profile(int enable) = 0;
+  virtual int profile_read(double* ms, int64_t* count, int n) = 0;
   int64_t bytes = 0;
   double shift[3] = {0, 0, 0};
   std::vector<int32_t> order;
@@ -167,8 +179,48 @@ struct Engine : EngineBase {
   double w3 = 1.0;
   unsigned int n_inside = 0;
 
+  // ---- measurement: named stream events and per-kernel launch timing ----
+  cudaEvent_t marks[8] = {};
+  bool profiling = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_open;
+  std::vector<cudaEvent_t> prof_pool;
+  double prof_ms[PROF_KINDS] = {};
+  int64_t prof_n[PROF_KINDS] = {};
+
+  cudaEvent_t pool_get() {
+    if (!prof_pool.empty()) { cudaEvent_t e = prof_pool.back(); prof_pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void pb(int kind) {
+    if (!profiling) return;
+    cudaEvent_t a = pool_get(), b = pool_get();
+    cudaEventRecord(a, st);
+    prof_open.push_back({kind, {a, b}});
+  }
+  void pe() {
+    if (!profiling || prof_open.empty()) return;
+    cudaEventRecord(prof_open.back().second.second, st);
+  }
+  void prof_collect() {
+    cudaStreamSynchronize(st);
+    for (auto& r : prof_open) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r.second.first, r.second.second);
+      prof_ms[r.first] += ms;
+      prof_n[r.first] += 1;
+      prof_pool.push_back(r.second.first);
+      prof_pool.push_back(r.second.second);
+    }
+    prof_open.clear();
+  }
+
   ~Engine() override {
     if (st) cudaStreamSynchronize(st);
+    for (auto& r : prof_open) { cudaEventDestroy(r.second.first); cudaEventDestroy(r.second.second); }
+    for (cudaEvent_t e : prof_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : marks) if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     if (st) cudaStreamDestroy(st);
   }
@@ -284,8 +336,9 @@ struct Engine : EngineBase {
     r |= alloc(d.staging_i, n);
     r |= alloc_shell(d.sh, cap);
     r |= alloc_shell(d.sh2, cap);
-    r |= alloc(d.dpos, 3 * ns); r |= alloc(d.dvel, 3 * ns); r |= alloc(d.dfrc, 3 * ns); r |= alloc(d.dq, 3 * ns);
-    r |= alloc(d.srel, ns); r |= alloc(d.facc, 4 * ns); r |= alloc(d.fmot, 4 * ns); r |= alloc(d.dpot, c.n_dimers);
+    const int64_t ns1 = std::max<int64_t>(ns, 1), nd1 = std::max<int64_t>(c.n_dimers, 1);
+    r |= alloc(d.dpos, 3 * ns1); r |= alloc(d.dvel, 3 * ns1); r |= alloc(d.dfrc, 3 * ns1); r |= alloc(d.dq, 3 * ns1);
+    r |= alloc(d.srel, ns1); r |= alloc(d.facc, 4 * ns1); r |= alloc(d.fmot, 4 * ns1); r |= alloc(d.dpot, nd1);
     int64_t nbins = (int64_t)kp.nbx * kp.nby * kp.nbz;
     r |= alloc(d.bin_cnt, nbins); r |= alloc(d.bin_list, nbins * BIN_SLOTS);
     if (sizeof(T) == 4) { float4* a = nullptr; r |= alloc(a, kp.ncell_shift); d.acc = a; }
@@ -439,18 +492,18 @@ struct Engine : EngineBase {
     StepArgs a = args(n);
     a.tc = tc;
     a.mpc = mpc ? 1 : 0;
-    Launch<T>::build_bins(d, kp, st);
+    pb(PROF_BINS); Launch<T>::build_bins(d, kp, st); pe();
     bool sort_now = cfg.sort_every > 0 && n % cfg.sort_every == 0;
     if (sort_now) {
       StepArgs m = a;
       m.merge_only = 1;
       m.mpc = 0;
-      Launch<T>::rebuild(d, kp, m, st);
-      Launch<T>::sort(d, kp, st);
+      pb(PROF_REBUILD); Launch<T>::rebuild(d, kp, m, st); pe();
+      pb(PROF_SORT); Launch<T>::sort(d, kp, st); pe();
       a.tc = 0;
     }
-    Launch<T>::rebuild(d, kp, a, st);
-    Launch<T>::finalize_rebuild(d, kp, a, cfg.skin, st);
+    pb(PROF_REBUILD); Launch<T>::rebuild(d, kp, a, st); pe();
+    pb(PROF_FINALIZE); Launch<T>::finalize_rebuild(d, kp, a, cfg.skin, st); pe();
     Counters h;
     int r = read_counters(h);
     if (r) return r;
@@ -517,8 +570,8 @@ struct Engine : EngineBase {
       if (!advanced) {
         StepArgs a = args(n - 1);
         a.advance = 1;
-        Launch<T>::advance(d, kp, a, st);
-        Launch<T>::dimer(d, kp, a, 2, w3, cfg.rattle_max_iter, st);
+        pb(PROF_SHELL_ADVANCE); Launch<T>::advance(d, kp, a, st); pe();
+        pb(PROF_DIMER); Launch<T>::dimer(d, kp, a, 2, w3, cfg.rattle_max_iter, st); pe();
         advanced = true;
       }
       time_count += 1;
@@ -542,13 +595,15 @@ struct Engine : EngineBase {
       a.mpc = mpc ? 1 : 0;
       a.rebuilt = rebuild ? 1 : 0;
       a.advance = last ? 0 : 1;
-      Launch<T>::force(d, kp, a, st);
-      if (mpc && kp.kinetics == MPCMD_KIN_SELKOV && kp.exclusion == MPCMD_EXCL_CELLS) Launch<T>::affected(d, kp, a, st);
-      Launch<T>::dimer(d, kp, a, 1 | (last ? 0 : 2), w3, cfg.rattle_max_iter, st);
+      pb(PROF_FORCE); Launch<T>::force(d, kp, a, st); pe();
+      if (mpc && kp.kinetics == MPCMD_KIN_SELKOV && kp.exclusion == MPCMD_EXCL_CELLS) {
+        pb(PROF_AFFECTED); Launch<T>::affected(d, kp, a, st); pe();
+      }
+      pb(PROF_DIMER); Launch<T>::dimer(d, kp, a, 1 | (last ? 0 : 2), w3, cfg.rattle_max_iter, st); pe();
       if (mpc) {
-        Launch<T>::cells(d, kp, a, 1 | (kp.kinetics ? 2 : 0), st);
-        Launch<T>::rotate_main(d, kp, a, st);
-        Launch<T>::rotate_shell(d, kp, a, st);
+        pb(PROF_CELLS); Launch<T>::cells(d, kp, a, 1 | (kp.kinetics ? 2 : 0), st); pe();
+        pb(PROF_ROTATE_MAIN); Launch<T>::rotate_main(d, kp, a, st); pe();
+        pb(PROF_SHELL_ADVANCE); Launch<T>::rotate_shell(d, kp, a, st); pe();
       }
       advanced = !last;
       cstep = n;
@@ -668,7 +723,7 @@ struct Engine : EngineBase {
           if (per) P[u][2] = wrapf(P[u][2], L[2]);
         }
         bool bad = false;
-        if (!per)
+        if (!per && !cfg.init_plane)
           bad = P[0][2] < wcC + rc * cut || P[0][2] > L[2] - wcC - rc * cut || P[1][2] < wcN + rn * cut ||
                 P[1][2] > L[2] - wcN - rn * cut;
         for (int j = 0; j < i && !bad; ++j)
@@ -676,7 +731,8 @@ struct Engine : EngineBase {
             for (int v = 0; v < 2 && !bad; ++v) {
               double dd[3];
               for (int q = 0; q < 3; ++q) dd[q] = P[u][q] - pos[3 * (2 * j + v) + q];
-              if (per) for (int q = 0; q < 3; ++q) dd[q] = mi(dd[q], L[q]);
+              // minimum image in the periodic directions (x, y always; z when periodic)
+              for (int q = 0; q < (per ? 3 : 2); ++q) dd[q] = mi(dd[q], L[q]);
               double r = (u == 0 ? rc : rn) + (v == 0 ? rc : rn);
               double lim = (r * cut) * (r * cut);
               if (u == 0 && v == 0) lim = (2. * rc * cut) * (2. * rc * cut);
@@ -837,6 +893,36 @@ struct Engine : EngineBase {
 
   int checkpoint(const char* path) override;
   int restore(const char* path) override;
+
+  int event_record(int slot) override {
+    if (slot < 0 || slot >= 8) return MPCMD_ERR_CONFIG;
+    if (!marks[slot]) CK(cudaEventCreate(&marks[slot]));
+    CK(cudaEventRecord(marks[slot], st));
+    return MPCMD_OK;
+  }
+  int event_elapsed(int a, int b, double* ms) override {
+    if (a < 0 || a >= 8 || b < 0 || b >= 8 || !marks[a] || !marks[b]) return MPCMD_ERR_STATE;
+    CK(cudaEventSynchronize(marks[b]));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, marks[a], marks[b]));
+    *ms = f;
+    return MPCMD_OK;
+  }
+  int synchronize() override {
+    CK(cudaStreamSynchronize(st));
+    return MPCMD_OK;
+  }
+  int profile(int enable) override {
+    prof_collect();
+    profiling = enable != 0;
+    if (enable) for (int k = 0; k < PROF_KINDS; ++k) { prof_ms[k] = 0.; prof_n[k] = 0; }
+    return MPCMD_OK;
+  }
+  int profile_read(double* ms, int64_t* count, int n) override {
+    prof_collect();
+    for (int k = 0; k < n && k < PROF_KINDS; ++k) { ms[k] = prof_ms[k]; count[k] = prof_n[k]; }
+    return MPCMD_OK;
+  }
 };
 
 // ------------------------------------------------------- checkpoint ----
@@ -925,6 +1011,7 @@ extern "C" {
 int mpcmd_create(const mpcmd_config* cfg, mpcmd_ctx** out) {
   if (!cfg || !out) return MPCMD_ERR_CONFIG;
   *out = nullptr;
+  cudaGetLastError();
   std::unique_ptr<mpcmd_ctx> c(new mpcmd_ctx);
   if (cfg->precision == MPCMD_PREC_FP64) c->e.reset(new Engine<double>());
   else if (cfg->precision == MPCMD_PREC_FP32 || cfg->precision == 0) c->e.reset(new Engine<float>());
@@ -957,7 +1044,13 @@ const char* mpcmd_error_string(int s) {
   }
 }
 
-#define CTX_OK(ctx) if (!(ctx) || !(ctx)->e) return MPCMD_ERR_STATE
+// Every entry point first clears a stale CUDA error of this thread (left by
+// another context or library) so launch errors are attributed to this call.
+#define CTX_OK(ctx)                               \
+  do {                                            \
+    if (!(ctx) || !(ctx)->e) return MPCMD_ERR_STATE; \
+    cudaGetLastError();                           \
+  } while (0)
 
 int mpcmd_device_bytes(const mpcmd_ctx* ctx, int64_t* bytes) {
   CTX_OK(ctx);
@@ -1056,6 +1149,23 @@ int mpcmd_cell_order(mpcmd_ctx* ctx, int32_t* order) {
 int64_t mpcmd_kernel_launches(mpcmd_ctx* ctx) {
   (void)ctx;
   return mpcmd::g_kernel_launches;
+}
+int mpcmd_set_device(int device) {
+  if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return MPCMD_ERR_CUDA; }
+  return MPCMD_OK;
+}
+int mpcmd_event_record(mpcmd_ctx* ctx, int slot) { CTX_OK(ctx); return ctx->e->event_record(slot); }
+int mpcmd_event_elapsed(mpcmd_ctx* ctx, int a, int b, double* ms) {
+  CTX_OK(ctx);
+  if (!ms) return MPCMD_ERR_CONFIG;
+  return ctx->e->event_elapsed(a, b, ms);
+}
+int mpcmd_synchronize(mpcmd_ctx* ctx) { CTX_OK(ctx); return ctx->e->synchronize(); }
+int mpcmd_profile(mpcmd_ctx* ctx, int enable) { CTX_OK(ctx); return ctx->e->profile(enable); }
+int mpcmd_profile_read(mpcmd_ctx* ctx, double* ms, int64_t* count, int n) {
+  CTX_OK(ctx);
+  if (!ms || !count) return MPCMD_ERR_CONFIG;
+  return ctx->e->profile_read(ms, count, n);
 }
 double mpcmd_contract_u01(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra, uint32_t step, int which) {
   double u0, u1;

@@ -118,8 +118,7 @@ __global__ void k_upload_pos(Particles<T> p, KParams<T> kp, const double* v, int
     T o = (T)(x - f);
     if (o >= (T)1) { o -= (T)1; c += 1; }
     if (comp < 2 || kp.geometry == 1) {
-      while (c >= L) c -= L;
-      while (c < 0) c += L;
+      c = wrap_cell(c, L);
     } else {
       if (c >= L) { c = L - 1; o = (T)1; }
       if (c < 0) { c = 0; o = (T)0; }
@@ -254,7 +253,7 @@ __device__ __forceinline__ bool bin_first(int c, int lo, int L, bool wraps, int&
 
 template <typename T>
 __global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.x;
   if (s >= kp.ns) return;
   const double R = (s & 1) ? Rn : Rc;
   int lo[3], hi[3];
@@ -262,27 +261,20 @@ __global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn) {
   const int L[3] = {kp.lx, kp.ly, kp.lz};
   const bool per[3] = {true, true, kp.geometry == 1};
   for (int q = 0; q < 3; ++q) wr[q] = axis_range(d.dpos[3 * s + q], R, L[q], per[q], lo[q], hi[q]);
-#ifdef MPCMD_CHECKED
-  if (s < 2)
-    for (int q = 0; q < 3; ++q) { d.ctr->sums[6 * s + 2 * q] = (double)lo[q]; d.ctr->sums[6 * s + 2 * q + 1] = (double)hi[q]; }
-#endif
+  const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+  const int tot = nx * ny * nz;
   const int nbins = kp.nbx * kp.nby * kp.nbz;
-  for (int cx = lo[0]; cx <= hi[0]; ++cx) {
-    int bx;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int cx = lo[0] + t % nx, cy = lo[1] + (t / nx) % ny, cz = lo[2] + t / (nx * ny);
+    int bx, by, bz;
     if (!bin_first(cx, lo[0], L[0], wr[0], bx)) continue;
-    for (int cy = lo[1]; cy <= hi[1]; ++cy) {
-      int by;
-      if (!bin_first(cy, lo[1], L[1], wr[1], by)) continue;
-      for (int cz = lo[2]; cz <= hi[2]; ++cz) {
-        int bz;
-        if (!bin_first(cz, lo[2], L[2], wr[2], bz)) continue;
-        int bin = bx + kp.nbx * (by + kp.nby * bz);
-        if (!chk(bin >= 0 && bin < nbins, d.ctr, 108, bin)) continue;
-        unsigned int slot = atomicAdd(&d.bin_cnt[bin], 1u);
-        if (slot < (unsigned)BIN_SLOTS) d.bin_list[(size_t)bin * BIN_SLOTS + slot] = (uint16_t)s;
-        else atomicOr(&d.ctr->status, DEV_ERR_BIN_OVERFLOW);
-      }
-    }
+    if (!bin_first(cy, lo[1], L[1], wr[1], by)) continue;
+    if (!bin_first(cz, lo[2], L[2], wr[2], bz)) continue;
+    int bin = bx + kp.nbx * (by + kp.nby * bz);
+    if (!chk(bin >= 0 && bin < nbins, d.ctr, 108, bin)) continue;
+    unsigned int slot = atomicAdd(&d.bin_cnt[bin], 1u);
+    if (slot < (unsigned)BIN_SLOTS) d.bin_list[(size_t)bin * BIN_SLOTS + slot] = (uint16_t)s;
+    else atomicOr(&d.ctr->status, DEV_ERR_BIN_OVERFLOW);
   }
 }
 
@@ -307,7 +299,7 @@ void Launch<T>::build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t s
   cudaMemsetAsync(d.bin_cnt, 0, sizeof(uint32_t) * nbins, st);
   if (kp.ns == 0) return;
   double Rc = sqrt((double)kp.full2[0]) + 1e-6, Rn = sqrt((double)kp.full2[1]) + 1e-6;
-  k_bins_fill<T><<<(kp.ns + 63) / 64, 64, 0, st>>>(d, kp, Rc, Rn);
+  k_bins_fill<T><<<kp.ns, 128, 0, st>>>(d, kp, Rc, Rn);
   k_bins_sort<T><<<(nbins + 255) / 256, 256, 0, st>>>(d, nbins);
   LAUNCH_COUNT(); LAUNCH_COUNT();
 }

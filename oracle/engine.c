@@ -470,7 +470,7 @@ int orc_initial(orc_t* o) {
       if (periodic) { Z1 = wrap_floor(Z1, o->L[2]); Z2 = wrap_floor(Z2, o->L[2]); }
       double P[2][3] = {{X1, Y1, Z1}, {X2, Y2, Z2}};
       int bad = 0;
-      if (!periodic) {
+      if (!periodic && !o->p.init_plane) {
         bad = Z1 < sqrt(wcC2) + rc * cut || Z1 > o->L[2] - sqrt(wcC2) - rc * cut ||
               Z2 < sqrt(wcN2) + rn * cut || Z2 > o->L[2] - sqrt(wcN2) - rn * cut;
       }
@@ -479,7 +479,10 @@ int orc_initial(orc_t* o) {
           for (int v = 0; v < 2 && !bad; ++v) {
             double d[3];
             for (int c = 0; c < 3; ++c) d[c] = P[u][c] - o->dpos[3 * (2 * j + v) + c];
-            if (periodic) for (int c = 0; c < 3; ++c) d[c] = pbc_d(d[c], o->L[c]);
+            /* minimum image in the periodic directions (initial_mod.f95:108-111
+             * compares raw differences, which lets dimers overlap across the
+             * periodic x/y boundary) */
+            for (int c = 0; c < (periodic ? 3 : 2); ++c) d[c] = pbc_d(d[c], o->L[c]);
             double r = (u == 0 ? rc : rn) + (v == 0 ? rc : rn);
             double lim = (r * cut) * (r * cut);
             if (u == 0 && v == 0) lim = (2. * rc * cut) * (2. * rc * cut);
