@@ -71,6 +71,23 @@ MPCMD_HD void contract_bits(uint64_t seed, uint32_t tag, uint32_t index, uint32_
   m1 = ((uint64_t)c2 << 21) | (uint64_t)(c3 >> 11);
 }
 
+// Leading 32-bit word of draw `which` (0: words 0-1, 1: words 2-3): the top
+// bits of the 53-bit uniform of contract_pair.
+MPCMD_HD uint32_t index_word(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
+                             uint32_t step, int which) {
+  uint32_t c0 = index, c1 = extra, c2 = step, c3 = tag;
+  philox4x32_10(c0, c1, c2, c3, (uint32_t)seed, (uint32_t)(seed >> 32));
+  return which ? c2 : c0;
+}
+
+// Integer threshold of a probability p for draws compared as `p > u`:
+// p > m / 2^53  <=>  m < ceil(p 2^53)  (m the 53-bit mantissa).
+inline uint64_t prob_threshold(double p) {
+  if (!(p > 0.0)) return 0ull;
+  if (p >= 1.0) return 1ull << 53;
+  return (uint64_t)ceil(p * 9007199254740992.0);
+}
+
 // ------------------------------------------------------------- cells ------
 MPCMD_HD uint32_t pack_cell(int x, int y, int z) {
   return (uint32_t)x | ((uint32_t)y << 10) | ((uint32_t)z << 20);
@@ -100,6 +117,7 @@ struct KParams {
   T msd_thr;             // (0.5 skin)^2
   T cosrot, sinrot;
   double rp_ab, rp_ba;
+  uint64_t thr_ab, thr_ba;   // integer thresholds of rp_ab / rp_ba on the 53-bit draws
   double tau;            // MPC interval
   double k[6];
   double dtd;            // MD step in FP64

@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mpcmd.h"
+#include "mpcmd.h"
 #include "mpcmd_engine.cuh"
 
 using namespace mpcmd;
@@ -170,7 +170,7 @@ struct Engine : EngineBase {
   KParams<T> kp{};
   cudaStream_t st = nullptr;
   std::vector<void*> allocs;
-  int grid = 0;
+  int grid = 0, g_rebuild = 0, g_force = 0, g_rotate = 0;
   int64_t cstep = 0;
   int time_count = 0, time_penetrate = 0;
   int64_t last_rebuild = 0;
@@ -268,6 +268,13 @@ struct Engine : EngineBase {
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     grid = nsm * 8;
+    // the heavy persistent kernels run exactly one wave: SMs x resident blocks
+    int occ[3];
+    Launch<T>::occupancy(occ);
+    CK(cudaGetLastError());
+    g_rebuild = nsm * std::max(occ[0], 1);
+    g_force = nsm * std::max(occ[1], 1);
+    g_rotate = nsm * std::max(occ[2], 1);
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
 
     const int64_t n = c.n_solvent, ns = 2 * (int64_t)c.n_dimers;
@@ -302,6 +309,8 @@ struct Engine : EngineBase {
     kp.cosrot = (T)std::cos(c.rot_angle);
     kp.sinrot = (T)std::sin(c.rot_angle);
     kp.rp_ab = c.rp_ab; kp.rp_ba = c.rp_ba;
+    kp.thr_ab = prob_threshold(c.rp_ab);
+    kp.thr_ba = prob_threshold(c.rp_ba);
     kp.tau = c.mpc_dt;
     for (int q = 0; q < 6; ++q) kp.k[q] = c.k[q];
     kp.nbx = (c.lx + BIN_EDGE - 1) / BIN_EDGE;
@@ -470,6 +479,7 @@ struct Engine : EngineBase {
     StepArgs a{};
     a.step = (uint32_t)step;
     a.grid = grid;
+    a.g_rebuild = g_rebuild; a.g_force = g_force; a.g_rotate = g_rotate;
     a.shift[0] = shift[0]; a.shift[1] = shift[1]; a.shift[2] = shift[2];
     return a;
   }

@@ -108,7 +108,10 @@ struct StepArgs {
   int advance;         // fuse kick1 + stream of the next step
   int rebuilt;         // a rebuild ran in this step
   int merge_only;      // rebuild pass: lazy-stream and merge only, no lists
-  int grid;            // persistent grid size
+  int grid;            // persistent grid size of the light kernels
+  int g_rebuild;       // SMs x resident blocks of k_rebuild, k_force, k_rotate_main
+  int g_force;
+  int g_rotate;
   double shift[3];     // collision grid shift of this step
 };
 
@@ -136,6 +139,8 @@ struct Launch {
   static void regather(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, cudaStream_t st);
+  // resident blocks per SM of the persistent kernels (rebuild, force, rotate)
+  static void occupancy(int* blocks);
   static void init_solvent(const Dev<T>& d, const KParams<T>& kp, const int64_t* bounds, double kT,
                            const double* mass, cudaStream_t st);
 };

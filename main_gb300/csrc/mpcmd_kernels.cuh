@@ -63,6 +63,35 @@ __device__ __forceinline__ void block_max_to(unsigned long long* target, double 
   }
 }
 
+// Sum of (fx, fy, fz, u) over the lanes of a converged warp that hold the same
+// sphere s (s < 0: nothing), added once per distinct sphere to facc[4s..4s+3].
+template <typename T>
+__device__ __forceinline__ void warp_sphere_add(double* facc, int s, T fx, T fy, T fz, T u) {
+  const unsigned full = 0xffffffffu;
+  unsigned remaining = __ballot_sync(full, s >= 0);
+  const int lane = threadIdx.x & 31;
+  while (remaining) {
+    const int src = __ffs(remaining) - 1;
+    const int sr = __shfl_sync(full, s, src);
+    const unsigned grp = __ballot_sync(full, s == sr);
+    T a0 = s == sr ? fx : (T)0, a1 = s == sr ? fy : (T)0, a2 = s == sr ? fz : (T)0, a3 = s == sr ? u : (T)0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(full, a0, o);
+      a1 += __shfl_xor_sync(full, a1, o);
+      a2 += __shfl_xor_sync(full, a2, o);
+      a3 += __shfl_xor_sync(full, a3, o);
+    }
+    if (lane == src) {
+      atomicAdd(&facc[4 * sr + 0], (double)a0);
+      atomicAdd(&facc[4 * sr + 1], (double)a1);
+      atomicAdd(&facc[4 * sr + 2], (double)a2);
+      atomicAdd(&facc[4 * sr + 3], (double)a3);
+    }
+    remaining &= ~grp;
+  }
+}
+
 // LJ 12-6 cut and shifted (forces_mod.f95:82-92).
 template <typename T>
 __device__ __forceinline__ void lj(const KParams<T>& kp, int t, T E, T dRsq, T dx, T dy, T dz,
@@ -315,108 +344,216 @@ __device__ __forceinline__ int bin_of(int lx, int ly, int nbx, int nby, uint32_t
 // pairs for every particle (neighbour_list + inout_particle_list), max v^2 for
 // time_penetrate, and on collision steps the collision and distribute
 // accumulation of the particles that stay outside.
+// One pass over all particles at a neighbour-list rebuild
+// (evolve_mod.f95:465-564): lazy streaming of the outside particles by
+// time_count steps, merge of the shell buffer, shell membership and sphere
+// pairs for every particle (neighbour_list + inout_particle_list), max v^2 for
+// time_penetrate, and on collision steps the collision and distribute
+// accumulation of the particles that stay outside.
+// Shared-memory aggregation of the collision and distribute accumulations of
+// one block chunk (256 consecutive particles touch a few dozen cells): one
+// global atomic per distinct cell instead of one per particle.
+constexpr int AGG = 512;
+constexpr uint32_t AGG_EMPTY = 0xFFFFFFFFu;
+struct AggTables {
+  uint32_t ckey[AGG];
+  float cval[AGG][4];
+  uint32_t dkey[AGG];
+  uint32_t dcnt[AGG];
+  uint32_t dfirst[AGG][4];  // smallest particle index per species
+};
+
+__device__ __forceinline__ int agg_slot(uint32_t* keys, uint32_t key) {
+  int h = (int)((key * 2654435761u) >> 23) & (AGG - 1);
+  for (int probe = 0; probe < 64; ++probe) {
+    uint32_t k = keys[h];
+    if (k == key) return h;
+    if (k == AGG_EMPTY) {
+      k = atomicCAS(&keys[h], AGG_EMPTY, key);
+      if (k == AGG_EMPTY || k == key) return h;
+    }
+    h = (h + 1) & (AGG - 1);
+  }
+  return -1;
+}
+
+__device__ __forceinline__ void agg_clear(AggTables& t) {
+  for (int q = threadIdx.x; q < AGG; q += blockDim.x) {
+    t.ckey[q] = AGG_EMPTY;
+    t.cval[q][0] = t.cval[q][1] = t.cval[q][2] = t.cval[q][3] = 0.f;
+    t.dkey[q] = AGG_EMPTY;
+    t.dcnt[q] = 0u;
+    t.dfirst[q][0] = t.dfirst[q][1] = t.dfirst[q][2] = t.dfirst[q][3] = 0xFFFFFFFFu;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void agg_flush(AggTables& t, const Dev<T>& d, const KParams<T>& kp) {
+  for (int q = threadIdx.x; q < AGG; q += blockDim.x) {
+    uint32_t ck = t.ckey[q];
+    if (ck != AGG_EMPTY)
+      atomicAdd(reinterpret_cast<float4*>(d.acc) + ck, make_float4(t.cval[q][0], t.cval[q][1], t.cval[q][2], t.cval[q][3]));
+    uint32_t dk = t.dkey[q];
+    if (dk != AGG_EMPTY) {
+      uint32_t add = t.dcnt[q];
+      uint32_t old = atomicAdd(&d.dcnt[dk], add);
+      for (int sp = 0; sp < 4; ++sp) {
+        uint32_t a = (add >> (8 * sp)) & 255u, b = (old >> (8 * sp)) & 255u;
+        if (a && a + b > (uint32_t)kp.cell_capacity) atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
+        if (t.dfirst[q][sp] != 0xFFFFFFFFu)
+          atomicMin(&d.dfirst[4 * (size_t)dk + sp], dist_key(0, t.dfirst[q][sp], 0));
+      }
+    }
+  }
+}
+
+// One pass over all particles at a neighbour-list rebuild
+// (evolve_mod.f95:465-564): lazy streaming of the outside particles by
+// time_count steps, merge of the shell buffer, shell membership and sphere
+// pairs for every particle (neighbour_list + inout_particle_list), max v^2 for
+// time_penetrate, and on collision steps the collision and distribute
+// accumulation of the particles that stay outside.
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_rebuild(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
   const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
-  double vmax2 = 0.;
+  T vmax2 = (T)0;
+  const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
-    uint8_t f = d.p.flag[i];
-    uint32_t cell;
-    T ox, oy, oz, vx, vy, vz;
-    uint8_t sp;
-    if (f & FLAG_HOME_SHELL) {
-      uint32_t j = d.p.cell[i];
-      if (!chk((int64_t)j < d.sh.cap, d.ctr, 109, j)) continue;
-      cell = d.sh.cell[j];
-      ox = d.sh.ox[j]; oy = d.sh.oy[j]; oz = d.sh.oz[j];
-      vx = d.sh.vx[j]; vy = d.sh.vy[j]; vz = d.sh.vz[j];
-      sp = d.sh.flag[j] & FLAG_SPECIES;
-    } else {
-      cell = d.p.cell[i];
-      ox = d.p.ox[i]; oy = d.p.oy[i]; oz = d.p.oz[i];
-      vx = d.p.vx[i]; vy = d.p.vy[i]; vz = d.p.vz[i];
-      sp = f & FLAG_SPECIES;
-      if (!(f & FLAG_INLIST) && a.tc > 0) {
-        uint8_t ff = sp;
-        stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, ff, true, a.tc);
-        sp = ff & FLAG_SPECIES;
+  // warp-aligned grid-stride loop: the distribute counts are aggregated over
+  // the lanes of a warp that fall in the same cell
+  unsigned int pend_old = 0, pend_shift = 0, pend_cnt = 0;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < kp.n; base += stride) {
+    const int64_t i = base + lane;
+    bool dist = false;
+    uint32_t cid = 0;
+    uint8_t sp = 0;
+    if (i < kp.n) {
+      // all main-array loads issue together (no dependence on the flag)
+      uint8_t f = d.p.flag[i];
+      uint32_t cell = d.p.cell[i];
+      T ox = d.p.ox[i], oy = d.p.oy[i], oz = d.p.oz[i];
+      T vx = d.p.vx[i], vy = d.p.vy[i], vz = d.p.vz[i];
+      bool skip = false;
+      if (f & FLAG_HOME_SHELL) {
+        uint32_t j = cell;
+        if (!chk((int64_t)j < d.sh.cap, d.ctr, 109, j)) { skip = true; j = 0; }
+        cell = d.sh.cell[j];
+        ox = d.sh.ox[j]; oy = d.sh.oy[j]; oz = d.sh.oz[j];
+        vx = d.sh.vx[j]; vy = d.sh.vy[j]; vz = d.sh.vz[j];
+        sp = d.sh.flag[j] & FLAG_SPECIES;
+      } else {
+        sp = f & FLAG_SPECIES;
+        if (!(f & FLAG_INLIST) && a.tc > 0) {
+          uint8_t ff = sp;
+          stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, ff, true, a.tc);
+          sp = ff & FLAG_SPECIES;
+        }
       }
-    }
-    double v2 = (double)(vx * vx + vy * vy + vz * vz);
-    vmax2 = fmax(vmax2, v2);
-    if (a.merge_only) {
-      d.p.cell[i] = cell;
-      d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
-      d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
-      d.p.flag[i] = sp;
-      continue;
-    }
-    // candidate spheres of this particle's coarse bin
-    int np = 0;
-    bool nonbulk = false;
-    uint16_t sph[PAIRMAX];
-    if (kp.ns > 0) {
-      int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
-      if (!chk(bin >= 0 && bin < kp.nbx * kp.nby * kp.nbz, d.ctr, 110, (long long)cell)) continue;
-      unsigned int nc = d.bin_cnt[bin];
-      if (!chk(nc <= (unsigned)BIN_SLOTS, d.ctr, 111, nc)) nc = 0;
-      const uint16_t* bl = d.bin_list + (size_t)bin * BIN_SLOTS;
-      for (unsigned int q = 0; q < nc; ++q) {
-        int s = bl[q];
-        if (!chk(s < kp.ns, d.ctr, 112, s)) continue;
-        SphereRel<T> sr = d.srel[s];
-        T dx, dy, dz;
-        T d2 = sep2(kp, cell, ox, oy, oz, sr, dx, dy, dz);
-        if (d2 <= kp.full2[s & 1]) {
-          if (np < PAIRMAX) sph[np] = (uint16_t)s;
-          np++;
-          if (d2 <= kp.cut2[s & 1]) nonbulk = true;
+      T v2 = vx * vx + vy * vy + vz * vz;
+      vmax2 = v2 > vmax2 ? v2 : vmax2;
+      if (skip) {
+      } else if (a.merge_only) {
+        d.p.cell[i] = cell;
+        d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
+        d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
+        d.p.flag[i] = sp;
+      } else {
+        // candidate spheres of this particle's coarse bin
+        int np = 0;
+        bool nonbulk = false;
+        uint16_t sph[PAIRMAX];
+        if (kp.ns > 0) {
+          int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
+          bool okb = chk(bin >= 0 && bin < kp.nbx * kp.nby * kp.nbz, d.ctr, 110, (long long)cell);
+          unsigned int nc = okb ? d.bin_cnt[bin] : 0u;
+          if (!chk(nc <= (unsigned)BIN_SLOTS, d.ctr, 111, nc)) nc = 0;
+          const uint16_t* bl = d.bin_list + (size_t)(okb ? bin : 0) * BIN_SLOTS;
+          for (unsigned int q = 0; q < nc; ++q) {
+            int s = bl[q];
+            if (!chk(s < kp.ns, d.ctr, 112, s)) continue;
+            SphereRel<T> sr = d.srel[s];
+            T dx, dy, dz;
+            T d2 = sep2(kp, cell, ox, oy, oz, sr, dx, dy, dz);
+            if (d2 <= kp.full2[s & 1]) {
+              if (np < PAIRMAX) sph[np] = (uint16_t)s;
+              np++;
+              if (d2 <= kp.cut2[s & 1]) nonbulk = true;
+            }
+          }
+        }
+        if (np > PAIRMAX) { atomicOr(&d.ctr->status, DEV_ERR_PAIR_OVERFLOW); np = PAIRMAX; }
+        bool placed = false;
+        if (np > 0) {
+          cg::coalesced_group g = cg::coalesced_threads();
+          unsigned int bslot = 0;
+          if (g.thread_rank() == 0) bslot = atomicAdd(&d.ctr->n_inside_new, g.size());
+          bslot = g.shfl(bslot, 0);
+          unsigned int j = bslot + g.thread_rank();
+          if ((int64_t)j >= d.sh2.cap) {
+            atomicOr(&d.ctr->status, DEV_ERR_SHELL_OVERFLOW);
+          } else {
+            d.sh2.idx[j] = (uint32_t)i;
+            d.sh2.cell[j] = cell;
+            d.sh2.ox[j] = ox; d.sh2.oy[j] = oy; d.sh2.oz[j] = oz;
+            d.sh2.vx[j] = vx; d.sh2.vy[j] = vy; d.sh2.vz[j] = vz;
+            d.sh2.msd[j] = (T)0;
+            d.sh2.flag[j] = sp | FLAG_INLIST;
+            d.sh2.nonbulk[j] = nonbulk ? 1 : 0;
+            d.sh2.np[j] = (uint8_t)np;
+            uint16_t v[PAIRMAX];
+#pragma unroll
+            for (int q = 0; q < PAIRMAX; ++q) v[q] = q < np ? sph[q] : (uint16_t)0xFFFF;
+            uint4 packed;
+            packed.x = v[0] | ((uint32_t)v[1] << 16); packed.y = v[2] | ((uint32_t)v[3] << 16);
+            packed.z = v[4] | ((uint32_t)v[5] << 16); packed.w = v[6] | ((uint32_t)v[7] << 16);
+            *reinterpret_cast<uint4*>(d.sh2.sph + (size_t)j * PAIRMAX) = packed;
+            d.p.cell[i] = j;
+            d.p.flag[i] = sp | FLAG_INLIST | FLAG_HOME_SHELL;
+            placed = true;
+          }
+        }
+        if (!placed) {
+          d.p.cell[i] = cell;
+          d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
+          d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
+          d.p.flag[i] = sp;
+          if (a.mpc) {
+            uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
+            d.skey[i] = key;
+            accum_coll<T>(d.acc, key, vx, vy, vz);
+            dist = kp.kinetics != 0;
+            cid = unshifted_id(kp.lx, kp.ly, cell);
+          }
         }
       }
     }
-    if (np > PAIRMAX) { atomicOr(&d.ctr->status, DEV_ERR_PAIR_OVERFLOW); np = PAIRMAX; }
-    if (np > 0) {
-      cg::coalesced_group g = cg::coalesced_threads();
-      unsigned int base = 0;
-      if (g.thread_rank() == 0) base = atomicAdd(&d.ctr->n_inside_new, g.size());
-      base = g.shfl(base, 0);
-      unsigned int j = base + g.thread_rank();
-      if ((int64_t)j >= d.sh2.cap) {
-        atomicOr(&d.ctr->status, DEV_ERR_SHELL_OVERFLOW);
-        continue;
-      }
-      d.sh2.idx[j] = (uint32_t)i;
-      d.sh2.cell[j] = cell;
-      d.sh2.ox[j] = ox; d.sh2.oy[j] = oy; d.sh2.oz[j] = oz;
-      d.sh2.vx[j] = vx; d.sh2.vy[j] = vy; d.sh2.vz[j] = vz;
-      d.sh2.msd[j] = (T)0;
-      d.sh2.flag[j] = sp | FLAG_INLIST;
-      d.sh2.nonbulk[j] = nonbulk ? 1 : 0;
-      d.sh2.np[j] = (uint8_t)np;
-      for (int q = 0; q < PAIRMAX; ++q) d.sh2.sph[(size_t)j * PAIRMAX + q] = q < np ? sph[q] : (uint16_t)0xFFFF;
-      d.p.cell[i] = j;
-      d.p.flag[i] = sp | FLAG_INLIST | FLAG_HOME_SHELL;
-    } else {
-      d.p.cell[i] = cell;
-      d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
-      d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
-      d.p.flag[i] = sp;
-      if (a.mpc) {
-        uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
-        d.skey[i] = key;
-        accum_coll<T>(d.acc, key, vx, vy, vz);
-        if (kp.kinetics != 0) accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), sp, dist_key(0, (uint32_t)i, 0));
+    // distribute_mod.f95:95-182 counts and first members, one atomic per
+    // (cell, species) group of the warp; the group's lowest lane holds its
+    // smallest particle index
+    if (a.mpc && kp.kinetics != 0 && !a.merge_only) {
+      const unsigned long long mk = dist ? (((unsigned long long)cid << 2) | sp) : ~0ull;
+      const unsigned peers = __match_any_sync(0xffffffffu, mk);
+      if (dist && lane == __ffs(peers) - 1) {
+        // the count returned by this atomic is checked one iteration later,
+        // so that the warp does not wait for it
+        if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
+          atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
+        pend_cnt = __popc(peers);
+        pend_shift = 8 * sp;
+        pend_old = atomicAdd(&d.dcnt[cid], pend_cnt << pend_shift);
+        atomicMin(&d.dfirst[4 * (size_t)cid + sp], dist_key(0, (uint32_t)i, 0));
       }
     }
   }
-  block_max_to<T>(&d.ctr->maxv2, vmax2);
+  if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
+    atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
+  block_max_to<T>(&d.ctr->maxv2, (double)vmax2);
 }
 
 template <typename T>
 void Launch<T>::rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
-  k_rebuild<T><<<a.grid, TPB, 0, st>>>(d, kp, a);
+  k_rebuild<T><<<a.g_rebuild, TPB, 0, st>>>(d, kp, a);
   LAUNCH_COUNT();
 }
 
@@ -461,9 +598,9 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
       return;
     }
   }
-  if ((int)blockIdx.x >= a.grid) {
+  if ((int)blockIdx.x >= a.g_force) {
     // sphere-sphere forces: one warp per sphere s
-    int w = ((int)blockIdx.x - a.grid) * (TPB / 32) + (threadIdx.x >> 5);
+    int w = ((int)blockIdx.x - a.g_force) * (TPB / 32) + (threadIdx.x >> 5);
     int lane = threadIdx.x & 31;
     if (w >= kp.ns) return;
     const int s = w, ks = s >> 1, is = s & 1;
@@ -509,132 +646,116 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
     }
     return;
   }
-  // per-block accumulation of the sphere reactions (small open-addressing table)
-  __shared__ int hid[32];
-  __shared__ T hf[32][4];
-  if (threadIdx.x < 32) { hid[threadIdx.x] = -1; hf[threadIdx.x][0] = hf[threadIdx.x][1] = hf[threadIdx.x][2] = hf[threadIdx.x][3] = (T)0; }
-  __syncthreads();
   const unsigned int nin = d.ctr->n_inside;
-  const int64_t stride = (int64_t)a.grid * blockDim.x;
+  const int64_t stride = (int64_t)a.g_force * blockDim.x;
   const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
-  double msdmax = 0.;
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
-    uint32_t cell = d.sh.cell[j];
-    T ox = d.sh.ox[j], oy = d.sh.oy[j], oz = d.sh.oz[j];
-    T vx = d.sh.vx[j], vy = d.sh.vy[j], vz = d.sh.vz[j];
-    uint8_t fl = d.sh.flag[j];
-    const int np = d.sh.np[j];
-    const uint32_t idx = d.sh.idx[j];
-    T fpx[PAIRMAX], fpy[PAIRMAX], fpz[PAIRMAX];
+  const int lane = threadIdx.x & 31;
+  T msdmax = (T)0;
+  // warp-aligned grid-stride loop: a warp stays converged for the per-sphere
+  // warp reductions below
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < (int64_t)nin; base += stride) {
+    const int64_t j = base + lane;
+    const bool act = j < (int64_t)nin;
+    uint32_t cell = 0, idx = 0;
+    T ox = 0, oy = 0, oz = 0, vx = 0, vy = 0, vz = 0;
+    uint8_t fl = 0;
+    int np = 0;
     uint16_t sphl[PAIRMAX];
+    if (act) {
+      cell = d.sh.cell[j];
+      ox = d.sh.ox[j]; oy = d.sh.oy[j]; oz = d.sh.oz[j];
+      vx = d.sh.vx[j]; vy = d.sh.vy[j]; vz = d.sh.vz[j];
+      fl = d.sh.flag[j];
+      np = d.sh.np[j];
+      idx = d.sh.idx[j];
+      const uint4 packed = *reinterpret_cast<const uint4*>(d.sh.sph + (size_t)j * PAIRMAX);
+      sphl[0] = (uint16_t)(packed.x & 0xFFFFu); sphl[1] = (uint16_t)(packed.x >> 16);
+      sphl[2] = (uint16_t)(packed.y & 0xFFFFu); sphl[3] = (uint16_t)(packed.y >> 16);
+      sphl[4] = (uint16_t)(packed.z & 0xFFFFu); sphl[5] = (uint16_t)(packed.z >> 16);
+      sphl[6] = (uint16_t)(packed.w & 0xFFFFu); sphl[7] = (uint16_t)(packed.w >> 16);
+    }
+    T fpx[PAIRMAX], fpy[PAIRMAX], fpz[PAIRMAX];
 #pragma unroll
     for (int q = 0; q < PAIRMAX; ++q) {
       fpx[q] = fpy[q] = fpz[q] = (T)0;
-      sphl[q] = q < np ? d.sh.sph[(size_t)j * PAIRMAX + q] : (uint16_t)0xFFFF;
-    }
-#pragma unroll
-    for (int q = 0; q < PAIRMAX; ++q) {
-      if (q >= np) break;
-      const int s = sphl[q];
-      const int t = s & 1;
-      const SphereRel<T> sr = d.srel[s];
-      T dx, dy, dz;
-      T d2 = sep2(kp, cell, ox, oy, oz, sr, dx, dy, dz);
-      if (d2 <= kp.cut2[t]) {
-        int spc = fl & FLAG_SPECIES;
-        T E = (t == 0) ? kp.eps_c[spc] : kp.eps_n[spc];
-        if (t == 0) {
-          if (kp.catalysis == 0) {
-            if (spc == 0) { fl = (fl & ~FLAG_SPECIES) | 1; E = kp.eps_c[1]; }
-          } else if (spc == 0 || spc == 1) {
-            double u0, u1;
-            contract_pair(kp.seed, TAG_CAT, idx, (uint32_t)s, a.step, u0, u1);
-            if (spc == 0 && kp.rp_ab > u0) fl = (fl & ~FLAG_SPECIES) | 1;
-            if (spc == 1 && kp.rp_ba > u0) fl = (fl & ~FLAG_SPECIES) | 0;
+      if (!__any_sync(0xffffffffu, q < np)) break;
+      int s = (q < np) ? (int)sphl[q] : -1;
+      T fx = 0, fy = 0, fz = 0, u = 0;
+      if (s >= 0) {
+        const int t = s & 1;
+        const SphereRel<T> sr = d.srel[s];
+        T dx, dy, dz;
+        T d2 = sep2(kp, cell, ox, oy, oz, sr, dx, dy, dz);
+        if (d2 <= kp.cut2[t]) {
+          int spc = fl & FLAG_SPECIES;
+          T E = (t == 0) ? kp.eps_c[spc] : kp.eps_n[spc];
+          if (t == 0) {
+            if (kp.catalysis == 0) {
+              if (spc == 0) { fl = (fl & ~FLAG_SPECIES) | 1; E = kp.eps_c[1]; }
+            } else if (spc == 0 || spc == 1) {
+              uint64_t m0, m1;
+              contract_bits(kp.seed, TAG_CAT, idx, (uint32_t)s, a.step, m0, m1);
+              if (spc == 0 && m0 < kp.thr_ab) fl = (fl & ~FLAG_SPECIES) | 1;
+              if (spc == 1 && m0 < kp.thr_ba) fl = (fl & ~FLAG_SPECIES) | 0;
+            }
           }
-        }
-        T fx, fy, fz, u;
-        lj(kp, t, E, d2, dx, dy, dz, fx, fy, fz, u);
-        fpx[q] = fx; fpy[q] = fy; fpz[q] = fz;
-        // sphere reaction -F and potential into the block table
-        int h = s & 31;
-        bool done = false;
-        for (int probe = 0; probe < 32 && !done; ++probe) {
-          int cur = hid[h];
-          if (cur == -1) cur = atomicCAS(&hid[h], -1, s);
-          if (cur == -1 || cur == s) {
-            atomicAdd(&hf[h][0], -fx);
-            atomicAdd(&hf[h][1], -fy);
-            atomicAdd(&hf[h][2], -fz);
-            atomicAdd(&hf[h][3], u);
-            done = true;
-          } else {
-            h = (h + 1) & 31;
-          }
-        }
-        if (!done) {
-          atomicAdd(&d.facc[4 * s + 0], -(double)fx);
-          atomicAdd(&d.facc[4 * s + 1], -(double)fy);
-          atomicAdd(&d.facc[4 * s + 2], -(double)fz);
-          atomicAdd(&d.facc[4 * s + 3], (double)u);
+          lj(kp, t, E, d2, dx, dy, dz, fx, fy, fz, u);
+        } else {
+          s = -1;   // in the skin only: no contribution
         }
       }
+      fpx[q] = fx; fpy[q] = fy; fpz[q] = fz;
+      warp_sphere_add(d.facc, s, -fx, -fy, -fz, u);
     }
-    const T h2 = kp.hIM[fl & FLAG_SPECIES];
-#pragma unroll
-    for (int q = 0; q < PAIRMAX; ++q) {
-      if (q >= np) break;
-      vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
-    }
-    if (a.mpc) {
-      uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
-      d.sh.skey[j] = key;
-      accum_coll<T>(d.acc, key, vx, vy, vz);
-      if (kp.kinetics != 0) {
-        bool bulk = kp.exclusion == 1 || !d.sh.nonbulk[j];
-        if (bulk)
-          accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), fl & FLAG_SPECIES,
-                     dist_key(kp.exclusion == 0 ? 1 : 0, idx, (uint32_t)j + 1u));
-      }
-    }
-    if (a.advance && !a.mpc) {
+    if (act) {
+      const T h2 = kp.hIM[fl & FLAG_SPECIES];
 #pragma unroll
       for (int q = 0; q < PAIRMAX; ++q) {
         if (q >= np) break;
         vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
       }
-      stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
-      T msd = d.sh.msd[j] + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
-      d.sh.msd[j] = msd;
-      msdmax = fmax(msdmax, (double)msd);
-      d.sh.cell[j] = cell;
-      d.sh.ox[j] = ox; d.sh.oy[j] = oy; d.sh.oz[j] = oz;
-    } else {
-#pragma unroll
-      for (int q = 0; q < PAIRMAX; ++q) {
-        if (q >= np) break;
-        size_t b = ((size_t)j * PAIRMAX + q) * 3;
-        d.sh.pf[b] = fpx[q]; d.sh.pf[b + 1] = fpy[q]; d.sh.pf[b + 2] = fpz[q];
+      if (a.mpc) {
+        uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
+        d.sh.skey[j] = key;
+        accum_coll<T>(d.acc, key, vx, vy, vz);
+        if (kp.kinetics != 0) {
+          bool bulk = kp.exclusion == 1 || !d.sh.nonbulk[j];
+          if (bulk)
+            accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), fl & FLAG_SPECIES,
+                       dist_key(kp.exclusion == 0 ? 1 : 0, idx, (uint32_t)j + 1u));
+        }
       }
+      if (a.advance && !a.mpc) {
+#pragma unroll
+        for (int q = 0; q < PAIRMAX; ++q) {
+          if (q >= np) break;
+          vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
+        }
+        stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
+        T msd = d.sh.msd[j] + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
+        d.sh.msd[j] = msd;
+        msdmax = msd > msdmax ? msd : msdmax;
+        d.sh.cell[j] = cell;
+        d.sh.ox[j] = ox; d.sh.oy[j] = oy; d.sh.oz[j] = oz;
+      } else {
+#pragma unroll
+        for (int q = 0; q < PAIRMAX; ++q) {
+          if (q >= np) break;
+          size_t bq = ((size_t)j * PAIRMAX + q) * 3;
+          d.sh.pf[bq] = fpx[q]; d.sh.pf[bq + 1] = fpy[q]; d.sh.pf[bq + 2] = fpz[q];
+        }
+      }
+      d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
+      d.sh.flag[j] = fl;
     }
-    d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
-    d.sh.flag[j] = fl;
   }
-  if (a.advance && !a.mpc) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], msdmax);
-  __syncthreads();
-  if (threadIdx.x < 32 && hid[threadIdx.x] >= 0) {
-    int s = hid[threadIdx.x];
-    atomicAdd(&d.facc[4 * s + 0], (double)hf[threadIdx.x][0]);
-    atomicAdd(&d.facc[4 * s + 1], (double)hf[threadIdx.x][1]);
-    atomicAdd(&d.facc[4 * s + 2], (double)hf[threadIdx.x][2]);
-    atomicAdd(&d.facc[4 * s + 3], (double)hf[threadIdx.x][3]);
-  }
+  if (a.advance && !a.mpc) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], (double)msdmax);
 }
 
 template <typename T>
 void Launch<T>::force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
   int extra = (kp.ns + (TPB / 32) - 1) / (TPB / 32);
-  k_force<T><<<a.grid + extra, TPB, 0, st>>>(d, kp, a);
+  k_force<T><<<a.g_force + extra, TPB, 0, st>>>(d, kp, a);
   LAUNCH_COUNT();
 }
 
@@ -646,7 +767,7 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
   if (d.ctr->abort_step) return;
   const unsigned int nin = d.ctr->n_inside;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  double msdmax = 0.;
+  T msdmax = (T)0;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
     T vx = d.sh.vx[j], vy = d.sh.vy[j], vz = d.sh.vz[j];
     if (rotate) {
@@ -666,14 +787,14 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
       stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
       T msd = d.sh.msd[j] + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
       d.sh.msd[j] = msd;
-      msdmax = fmax(msdmax, (double)msd);
+      msdmax = msd > msdmax ? msd : msdmax;
       d.sh.cell[j] = cell;
       d.sh.ox[j] = ox; d.sh.oy[j] = oy; d.sh.oz[j] = oz;
       d.sh.flag[j] = fl;
     }
     d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
   }
-  if (a.advance) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], msdmax);
+  if (a.advance) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], (double)msdmax);
 }
 
 template <typename T>
@@ -1009,14 +1130,18 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
       }
       T ux, uy, uz;
       if (sizeof(T) == 4) {
-        uint64_t m0, m1;
-        contract_bits(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, m0, m1);
-        float u1 = (float)(m0 >> 29) * (1.f / 16777216.f);
-        float u2 = (float)(m1 >> 29) * (1.f / 16777216.f);
+        // FP32 axis from the top 32 bits of each draw; the radius is
+        // 2 sqrt(u (1 - u)) = sqrt(1 - theta^2) with both factors at full
+        // relative precision (no cancellation near the poles)
+        uint32_t w0 = index_word(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, 0);
+        uint32_t w2 = index_word(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, 1);
+        const float two32 = 2.3283064365386963e-10f;
+        float u1 = (float)w0 * two32;
+        float u2 = (float)w2 * two32, v2 = ((float)(~w2) + 1.f) * two32;
         float sp, cp;
         sincospif(2.f * u1, &sp, &cp);
-        float th = 2.f * u2 - 1.f;
-        float r = sqrtf(fmaxf(1.f - th * th, 0.f));
+        float th = u2 - v2;
+        float r = 2.f * sqrtf(u2 * v2);
         ux = (T)(r * cp); uy = (T)(r * sp); uz = (T)th;
       } else {
         double u1, u2;
@@ -1082,9 +1207,10 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
   if (d.ctr->abort_step) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
-    if (d.p.flag[i] & FLAG_HOME_SHELL) continue;
-    uint32_t key = d.skey[i];
+    const uint8_t f = d.p.flag[i];
+    const uint32_t key = d.skey[i];
     T vx = d.p.vx[i], vy = d.p.vy[i], vz = d.p.vz[i];
+    if (f & FLAG_HOME_SHELL) continue;
     rotate_v(kp, d.rot + 6 * (size_t)key, vx, vy, vz);
     d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
   }
@@ -1092,8 +1218,16 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
 
 template <typename T>
 void Launch<T>::rotate_main(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
-  k_rotate_main<T><<<a.grid, TPB, 0, st>>>(d, kp, a);
+  k_rotate_main<T><<<a.g_rotate, TPB, 0, st>>>(d, kp, a);
   LAUNCH_COUNT();
+}
+
+template <typename T>
+void Launch<T>::occupancy(int* blocks) {
+  blocks[0] = blocks[1] = blocks[2] = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], k_rebuild<T>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], k_force<T>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], k_rotate_main<T>, TPB, 0);
 }
 
 // ---------------------------------------------------- shell home moves ----

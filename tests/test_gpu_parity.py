@@ -42,7 +42,8 @@ def test_collision_stage(case, prec):
             assert_close(se, so, cfg, pos=0.0, vel=1e-13)
         else:
             assert (kc_o != kc_e).mean() < 1e-4
-            assert np.abs(ax_e - ax_o).max() < 1e-5
+            # FP32 axis: 32-bit draws and float trigonometry, about 1e-7
+            assert np.abs(ax_e - ax_o).max() < 1e-6
             assert_close(se, so, cfg, pos=1e-6, vel=2e-5)
 
 
