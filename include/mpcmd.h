@@ -157,6 +157,34 @@ int mpcmd_synchronize(mpcmd_ctx* ctx);
 int mpcmd_profile(mpcmd_ctx* ctx, int enable);
 int mpcmd_profile_read(mpcmd_ctx* ctx, double* ms, int64_t* count, int n);
 
+/* Allocation-free collision ------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * a host whose memory manager owns all device memory (a pool sized at
+ * start-up or a framework allocator) and may not be bypassed, or a stepping
+ * loop that cannot pay cudaMalloc/cudaFree's device synchronisation.  It
+ * performs the FP64 collision stage of mpcmd_mpc_rotation (grid shift drawn
+ * for `step`, per shifted cell centre of mass and random axis, rotation by
+ * rot_angle) on caller-owned device arrays: x, y, z absolute positions in
+ * cell units (inputs) and vx, vy, vz velocities (rotated in place), n
+ * particles, box lx x ly x lz cells, geometry MPCMD_GEOM_*, rotation_sense
+ * +1 (Rodrigues form) or -1 (projection form), contract seed.  Launches on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) and does not wait.
+ * Allocates nothing: its only scratch is a static device array of
+ * MPCMD_STATIC_MAX_CELLS x 4 doubles (16 MiB) that every GPU loading this
+ * library holds until exit; boxes with more shifted cells (lx*ly*lz, or
+ * lx*ly*(lz+1) with walls) return MPCMD_ERR_CONFIG.  The first call on a
+ * device resolves the array's address (cudaGetSymbolAddress) and must come
+ * before any stream capture.  All calls on a device share the array (each
+ * clears what it uses): calls that overlap on the GPU race and must be
+ * serialised by the caller.  On MPCMD_ERR_CUDA the CUDA error is left for
+ * cudaGetLastError. */
+#define MPCMD_STATIC_MAX_CELLS 524288
+int mpcmd_collide_static(const double* x, const double* y, const double* z,
+                         double* vx, double* vy, double* vz, int64_t n,
+                         int32_t lx, int32_t ly, int32_t lz, int32_t geometry,
+                         double rot_angle, int32_t rotation_sense, uint64_t seed,
+                         int64_t step, void* stream);
+
 /* Contract random numbers (same streams as the engine), for checkers. */
 double mpcmd_contract_u01(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
                           uint32_t step, int which);

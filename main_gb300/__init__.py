@@ -88,6 +88,10 @@ SIGNATURES = {
     "mpcmd_profile": (C.c_int, [_P, C.c_int]),
     "mpcmd_profile_read": (C.c_int, [_P, _dp, _lp, C.c_int]),
     "mpcmd_contract_u01": (C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
+    # allocation-free collision on caller-owned device arrays (pointers as integers)
+    "mpcmd_collide_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_double, C.c_int32, C.c_uint64, C.c_int64, C.c_void_p]),
 }
 
 

@@ -19,6 +19,7 @@ UNITS = [
     ("mpcmd_kernels_f64.cu", ["--fmad=false"]),
     ("mpcmd_scan.cu", []),
     ("mpcmd_engine.cu", []),
+    ("mpcmd_static.cu", ["--fmad=false"]),
 ]
 HEADERS = ["mpcmd_device.cuh", "mpcmd_engine.cuh", "mpcmd_kernels.cuh"]
 
