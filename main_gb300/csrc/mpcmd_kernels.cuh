@@ -344,75 +344,6 @@ __device__ __forceinline__ int bin_of(int lx, int ly, int nbx, int nby, uint32_t
 // pairs for every particle (neighbour_list + inout_particle_list), max v^2 for
 // time_penetrate, and on collision steps the collision and distribute
 // accumulation of the particles that stay outside.
-// One pass over all particles at a neighbour-list rebuild
-// (evolve_mod.f95:465-564): lazy streaming of the outside particles by
-// time_count steps, merge of the shell buffer, shell membership and sphere
-// pairs for every particle (neighbour_list + inout_particle_list), max v^2 for
-// time_penetrate, and on collision steps the collision and distribute
-// accumulation of the particles that stay outside.
-// Shared-memory aggregation of the collision and distribute accumulations of
-// one block chunk (256 consecutive particles touch a few dozen cells): one
-// global atomic per distinct cell instead of one per particle.
-constexpr int AGG = 512;
-constexpr uint32_t AGG_EMPTY = 0xFFFFFFFFu;
-struct AggTables {
-  uint32_t ckey[AGG];
-  float cval[AGG][4];
-  uint32_t dkey[AGG];
-  uint32_t dcnt[AGG];
-  uint32_t dfirst[AGG][4];  // smallest particle index per species
-};
-
-__device__ __forceinline__ int agg_slot(uint32_t* keys, uint32_t key) {
-  int h = (int)((key * 2654435761u) >> 23) & (AGG - 1);
-  for (int probe = 0; probe < 64; ++probe) {
-    uint32_t k = keys[h];
-    if (k == key) return h;
-    if (k == AGG_EMPTY) {
-      k = atomicCAS(&keys[h], AGG_EMPTY, key);
-      if (k == AGG_EMPTY || k == key) return h;
-    }
-    h = (h + 1) & (AGG - 1);
-  }
-  return -1;
-}
-
-__device__ __forceinline__ void agg_clear(AggTables& t) {
-  for (int q = threadIdx.x; q < AGG; q += blockDim.x) {
-    t.ckey[q] = AGG_EMPTY;
-    t.cval[q][0] = t.cval[q][1] = t.cval[q][2] = t.cval[q][3] = 0.f;
-    t.dkey[q] = AGG_EMPTY;
-    t.dcnt[q] = 0u;
-    t.dfirst[q][0] = t.dfirst[q][1] = t.dfirst[q][2] = t.dfirst[q][3] = 0xFFFFFFFFu;
-  }
-}
-
-template <typename T>
-__device__ __forceinline__ void agg_flush(AggTables& t, const Dev<T>& d, const KParams<T>& kp) {
-  for (int q = threadIdx.x; q < AGG; q += blockDim.x) {
-    uint32_t ck = t.ckey[q];
-    if (ck != AGG_EMPTY)
-      atomicAdd(reinterpret_cast<float4*>(d.acc) + ck, make_float4(t.cval[q][0], t.cval[q][1], t.cval[q][2], t.cval[q][3]));
-    uint32_t dk = t.dkey[q];
-    if (dk != AGG_EMPTY) {
-      uint32_t add = t.dcnt[q];
-      uint32_t old = atomicAdd(&d.dcnt[dk], add);
-      for (int sp = 0; sp < 4; ++sp) {
-        uint32_t a = (add >> (8 * sp)) & 255u, b = (old >> (8 * sp)) & 255u;
-        if (a && a + b > (uint32_t)kp.cell_capacity) atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
-        if (t.dfirst[q][sp] != 0xFFFFFFFFu)
-          atomicMin(&d.dfirst[4 * (size_t)dk + sp], dist_key(0, t.dfirst[q][sp], 0));
-      }
-    }
-  }
-}
-
-// One pass over all particles at a neighbour-list rebuild
-// (evolve_mod.f95:465-564): lazy streaming of the outside particles by
-// time_count steps, merge of the shell buffer, shell membership and sphere
-// pairs for every particle (neighbour_list + inout_particle_list), max v^2 for
-// time_penetrate, and on collision steps the collision and distribute
-// accumulation of the particles that stay outside.
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_rebuild(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
