@@ -345,7 +345,7 @@ __device__ __forceinline__ int bin_of(int lx, int ly, int nbx, int nby, uint32_t
 // time_penetrate, and on collision steps the collision and distribute
 // accumulation of the particles that stay outside.
 template <typename T>
-__global__ void __launch_bounds__(TPB) k_rebuild(Dev<T> d, KParams<T> kp, StepArgs a) {
+__global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
   const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
   T vmax2 = (T)0;
@@ -365,6 +365,10 @@ __global__ void __launch_bounds__(TPB) k_rebuild(Dev<T> d, KParams<T> kp, StepAr
       uint32_t cell = d.p.cell[i];
       T ox = d.p.ox[i], oy = d.p.oy[i], oz = d.p.oz[i];
       T vx = d.p.vx[i], vy = d.p.vy[i], vz = d.p.vz[i];
+      const uint32_t cell0 = cell;
+      const T vx0 = vx, vy0 = vy, vz0 = vz;
+      const bool from_shell = (f & FLAG_HOME_SHELL) != 0;
+      const bool streamed = !from_shell && !(f & FLAG_INLIST) && a.tc > 0;
       bool skip = false;
       if (f & FLAG_HOME_SHELL) {
         uint32_t j = cell;
@@ -383,12 +387,20 @@ __global__ void __launch_bounds__(TPB) k_rebuild(Dev<T> d, KParams<T> kp, StepAr
       }
       T v2 = vx * vx + vy * vy + vz * vz;
       vmax2 = v2 > vmax2 ? v2 : vmax2;
+      // write back only what changed: a state merged from the shell in full;
+      // a lazily streamed particle its offsets, and its cell, velocity (wall
+      // bounce) and flag when they changed
+      const bool wr_all = from_shell;
+      const bool wr_cell = wr_all || cell != cell0;
+      const bool wr_pos = wr_all || streamed;
+      const bool wr_vel = wr_all || vx != vx0 || vy != vy0 || vz != vz0;
+      const bool wr_flag = wr_all || sp != f;
       if (skip) {
       } else if (a.merge_only) {
-        d.p.cell[i] = cell;
-        d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
-        d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
-        d.p.flag[i] = sp;
+        if (wr_cell) d.p.cell[i] = cell;
+        if (wr_pos) { d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz; }
+        if (wr_vel) { d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz; }
+        if (wr_flag) d.p.flag[i] = sp;
       } else {
         // candidate spheres of this particle's coarse bin
         int np = 0;
@@ -445,10 +457,10 @@ __global__ void __launch_bounds__(TPB) k_rebuild(Dev<T> d, KParams<T> kp, StepAr
           }
         }
         if (!placed) {
-          d.p.cell[i] = cell;
-          d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz;
-          d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
-          d.p.flag[i] = sp;
+          if (wr_cell) d.p.cell[i] = cell;
+          if (wr_pos) { d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz; }
+          if (wr_vel) { d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz; }
+          if (wr_flag) d.p.flag[i] = sp;
           if (a.mpc) {
             uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
             d.skey[i] = key;
@@ -775,34 +787,43 @@ __device__ __forceinline__ double dmin_image(double d, double L) {
   return d;
 }
 
-// One block per dimer (evolve_mod.f95:605-636 totals, :679-724 RATTLE
-// velocities, :320-417 RATTLE positions of the next step).
-// mode bit 0: finish the force step (totals + RATTLE-v); bit 1: RATTLE-x.
+// One thread per dimer (evolve_mod.f95:605-636 totals, :679-724 RATTLE
+// velocities, :320-417 RATTLE positions of the next step), on register copies
+// of the dimer state.  mode bit 0: finish the force step (totals +
+// RATTLE-v); bit 1: RATTLE-x.  The FP64 parity build performs the reference's
+// operation sequence; the FP32 production build multiplies by precomputed
+// reciprocals and wraps the positions once after the RATTLE-x iterations (the
+// constraint uses minimum-image separations, so the in-loop wraps of the
+// reference only change the stored result, which the final wrap reproduces).
 template <typename T>
 __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3, int rattle_max) {
   if (d.ctr->abort_step) return;
-  const int k = blockIdx.x;
-  if (k >= kp.nd || threadIdx.x != 0) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kp.nd) return;
+  constexpr bool fast = sizeof(T) == 4;
   const double dt = kp.dtd, Mc = kp.mc, Mn = kp.mn, Dcn = kp.dcn;
   const double hIMc = (0.5 * dt) / Mc, hIMn = (0.5 * dt) / Mn;
   const double IIM = 1.0 / ((1.0 / Mc) + (1.0 / Mn));
+  const double iMc = 1.0 / Mc, iMn = 1.0 / Mn, iD2 = 1.0 / (Dcn * Dcn);
+  const double iMcdt = 1.0 / (Mc * dt), iMndt = 1.0 / (Mn * dt);
   const bool per = kp.geometry == 1;
-  double* X1 = d.dpos + 3 * (2 * k);
-  double* X2 = d.dpos + 3 * (2 * k + 1);
-  double* V1 = d.dvel + 3 * (2 * k);
-  double* V2 = d.dvel + 3 * (2 * k + 1);
-  double* F1 = d.dfrc + 3 * (2 * k);
-  double* F2 = d.dfrc + 3 * (2 * k + 1);
-  double* Q1 = d.dq + 3 * (2 * k);
-  double* Q2 = d.dq + 3 * (2 * k + 1);
+  const int nwrap = per ? 3 : 2;
+  const int s1 = 2 * k, s2 = 2 * k + 1;
+  double X1[3], X2[3], V1[3], V2[3], F1[3], F2[3], Q1[3], Q2[3];
+  for (int c = 0; c < 3; ++c) {
+    X1[c] = d.dpos[3 * s1 + c]; X2[c] = d.dpos[3 * s2 + c];
+    V1[c] = d.dvel[3 * s1 + c]; V2[c] = d.dvel[3 * s2 + c];
+    F1[c] = d.dfrc[3 * s1 + c]; F2[c] = d.dfrc[3 * s2 + c];
+    Q1[c] = d.dq[3 * s1 + c]; Q2[c] = d.dq[3 * s2 + c];
+  }
   unsigned long long iters = 0;
   if (mode & 1) {
     double pot = 0.;
     for (int i = 0; i < 2; ++i) {
-      int s = 2 * k + i;
-      double* F = d.dfrc + 3 * s;
+      const int s = 2 * k + i;
+      double* F = i == 0 ? F1 : F2;
       double fw = 0., pw = 0.;
-      if (!per) lj_wall(kp, d.dpos[3 * s + 2], i == 0 ? kp.rwc : kp.rwn, w3, fw, pw);
+      if (!per) lj_wall(kp, (i == 0 ? X1 : X2)[2], i == 0 ? kp.rwc : kp.rwn, w3, fw, pw);
       F[0] = d.facc[4 * s + 0] + d.fmot[4 * s + 0];
       F[1] = d.facc[4 * s + 1] + d.fmot[4 * s + 1];
       F[2] = d.facc[4 * s + 2] + d.fmot[4 * s + 2] + fw;
@@ -821,14 +842,26 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
       double Con2diff = 2.0 * (dV[0] * dd[0] + dV[1] * dd[1] + dV[2] * dd[2]);
       if (fabs(Con2diff) < 1.e-8) break;
       if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
-      double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
-      for (int c = 0; c < 3; ++c) {
-        V1[c] = V1[c] + 2.0 * O * dd[c] / Mc;
-        V2[c] = V2[c] - 2.0 * O * dd[c] / Mn;
+      if (fast) {
+        const double O2 = -(0.5 * (IIM * Con2diff) * iD2);
+        for (int c = 0; c < 3; ++c) {
+          V1[c] = V1[c] + O2 * dd[c] * iMc;
+          V2[c] = V2[c] - O2 * dd[c] * iMn;
+        }
+      } else {
+        double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
+        for (int c = 0; c < 3; ++c) {
+          V1[c] = V1[c] + 2.0 * O * dd[c] / Mc;
+          V2[c] = V2[c] - 2.0 * O * dd[c] / Mn;
+        }
       }
       acc++;
     }
     iters += acc;
+    for (int c = 0; c < 3; ++c) {
+      d.dvel[3 * s1 + c] = V1[c]; d.dvel[3 * s2 + c] = V2[c];
+      d.dfrc[3 * s1 + c] = F1[c]; d.dfrc[3 * s2 + c] = F2[c];
+    }
   }
   if (mode & 2) {
     double pr1[3], pr2[3], dP[3];
@@ -838,9 +871,11 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
     if (per) dP[2] = dmin_image(dP[2], kp.Ld[2]);
     for (int c = 0; c < 3; ++c) { Q1[c] = V1[c] + hIMc * F1[c]; Q2[c] = V2[c] + hIMn * F2[c]; }
     for (int c = 0; c < 3; ++c) { X1[c] = X1[c] + dt * Q1[c]; X2[c] = X2[c] + dt * Q2[c]; }
-    for (int c = 0; c < (per ? 3 : 2); ++c) {
-      X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
-      X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+    if (!fast) {
+      for (int c = 0; c < nwrap; ++c) {
+        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+      }
     }
     int acc = 0;
     for (;;) {
@@ -853,29 +888,48 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
       if (fabs(Con1diff) < 1.e-6) break;
       if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
       double G = -(0.25 * Con1diff * IIM / (dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2]));
-      for (int c = 0; c < 3; ++c) {
-        X1[c] = pr1[c] + Q1[c] * dt + 2.0 * G * dP[c] / Mc;
-        X2[c] = pr2[c] + Q2[c] * dt - 2.0 * G * dP[c] / Mn;
-      }
-      for (int c = 0; c < (per ? 3 : 2); ++c) {
-        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
-        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
-      }
-      for (int c = 0; c < 3; ++c) {
-        Q1[c] = Q1[c] + 2.0 * G * dP[c] / (Mc * dt);
-        Q2[c] = Q2[c] - 2.0 * G * dP[c] / (Mn * dt);
+      if (fast) {
+        const double G2 = 2.0 * G;
+        for (int c = 0; c < 3; ++c) {
+          X1[c] = pr1[c] + Q1[c] * dt + G2 * dP[c] * iMc;
+          X2[c] = pr2[c] + Q2[c] * dt - G2 * dP[c] * iMn;
+          Q1[c] = Q1[c] + G2 * dP[c] * iMcdt;
+          Q2[c] = Q2[c] - G2 * dP[c] * iMndt;
+        }
+      } else {
+        for (int c = 0; c < 3; ++c) {
+          X1[c] = pr1[c] + Q1[c] * dt + 2.0 * G * dP[c] / Mc;
+          X2[c] = pr2[c] + Q2[c] * dt - 2.0 * G * dP[c] / Mn;
+        }
+        for (int c = 0; c < nwrap; ++c) {
+          X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+          X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+        }
+        for (int c = 0; c < 3; ++c) {
+          Q1[c] = Q1[c] + 2.0 * G * dP[c] / (Mc * dt);
+          Q2[c] = Q2[c] - 2.0 * G * dP[c] / (Mn * dt);
+        }
       }
       acc++;
     }
+    if (fast) {
+      for (int c = 0; c < nwrap; ++c) {
+        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+      }
+    }
     iters += acc;
+    for (int c = 0; c < 3; ++c) {
+      d.dpos[3 * s1 + c] = X1[c]; d.dpos[3 * s2 + c] = X2[c];
+      d.dq[3 * s1 + c] = Q1[c]; d.dq[3 * s2 + c] = Q2[c];
+    }
     for (int i = 0; i < 2; ++i) {
-      int s = 2 * k + i;
-      double XX = d.dpos[3 * s], YY = d.dpos[3 * s + 1], ZZ = d.dpos[3 * s + 2];
-      double fx = floor(XX), fy = floor(YY), fz = floor(ZZ);
+      const double* X = i == 0 ? X1 : X2;
+      const double fx = floor(X[0]), fy = floor(X[1]), fz = floor(X[2]);
       SphereRel<T> r;
       r.cx = (int)fx; r.cy = (int)fy; r.cz = (int)fz;
-      r.ox = (T)(XX - fx); r.oy = (T)(YY - fy); r.oz = (T)(ZZ - fz);
-      d.srel[s] = r;
+      r.ox = (T)(X[0] - fx); r.oy = (T)(X[1] - fy); r.oz = (T)(X[2] - fz);
+      d.srel[2 * k + i] = r;
     }
   }
   if (iters) atomicAdd(&d.ctr->rattle_iters, iters);
@@ -885,7 +939,7 @@ template <typename T>
 void Launch<T>::dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode, double w3,
                       int rattle_max, cudaStream_t st) {
   if (kp.nd == 0) return;
-  k_dimer<T><<<kp.nd, 32, 0, st>>>(d, kp, a, mode, w3, rattle_max);
+  k_dimer<T><<<(kp.nd + 63) / 64, 64, 0, st>>>(d, kp, a, mode, w3, rattle_max);
   LAUNCH_COUNT();
 }
 
@@ -1136,14 +1190,34 @@ void Launch<T>::cells(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, 
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
+  // two particles per thread and iteration: all loads and both table gathers
+  // are issued before the first store
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
-    const uint8_t f = d.p.flag[i];
-    const uint32_t key = d.skey[i];
-    T vx = d.p.vx[i], vy = d.p.vy[i], vz = d.p.vz[i];
-    if (f & FLAG_HOME_SHELL) continue;
-    rotate_v(kp, d.rot + 6 * (size_t)key, vx, vy, vz);
-    d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < kp.n; i0 += 2 * stride) {
+    const int64_t i1 = i0 + stride;
+    const bool h1 = i1 < kp.n;
+    const uint8_t f0 = d.p.flag[i0];
+    const uint8_t f1 = h1 ? d.p.flag[i1] : FLAG_HOME_SHELL;
+    const uint32_t k0 = d.skey[i0];
+    const uint32_t k1 = h1 ? d.skey[i1] : 0u;
+    T vx0 = d.p.vx[i0], vy0 = d.p.vy[i0], vz0 = d.p.vz[i0];
+    T vx1 = (T)0, vy1 = (T)0, vz1 = (T)0;
+    if (h1) { vx1 = d.p.vx[i1]; vy1 = d.p.vy[i1]; vz1 = d.p.vz[i1]; }
+    const bool r0 = !(f0 & FLAG_HOME_SHELL), r1 = !(f1 & FLAG_HOME_SHELL);
+    T t0[6], t1[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      t0[q] = r0 ? d.rot[6 * (size_t)k0 + q] : (T)0;
+      t1[q] = r1 ? d.rot[6 * (size_t)k1 + q] : (T)0;
+    }
+    if (r0) {
+      rotate_v(kp, t0, vx0, vy0, vz0);
+      d.p.vx[i0] = vx0; d.p.vy[i0] = vy0; d.p.vz[i0] = vz0;
+    }
+    if (r1) {
+      rotate_v(kp, t1, vx1, vy1, vz1);
+      d.p.vx[i1] = vx1; d.p.vy[i1] = vy1; d.p.vz[i1] = vz1;
+    }
   }
 }
 
