@@ -364,7 +364,7 @@ struct Engine : EngineBase {
 
     CK(cudaMemsetAsync(d.acc, 0, (sizeof(T) == 4 ? 16 : 32) * (size_t)kp.ncell_shift, st));
     CK(cudaMemsetAsync(d.dcnt, 0, 4 * (size_t)kp.ncell, st));
-    CK(cudaMemsetAsync(d.dfirst, 0xFF, 32 * (size_t)kp.ncell, st));
+    CK(cudaMemsetAsync(d.dfirst, 0xFF, 16 * (size_t)kp.ncell, st));
     CK(cudaMemsetAsync(d.affected, 0, (size_t)kp.ncell, st));
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
     CK(cudaMemsetAsync(d.facc, 0, sizeof(double) * 4 * std::max<int64_t>(ns, 1), st));
@@ -651,7 +651,7 @@ struct Engine : EngineBase {
     flush_shell();
     if (kp.ns > 0) Launch<T>::build_bins(d, kp, st);
     CK(cudaMemsetAsync(d.dcnt, 0, 4 * (size_t)kp.ncell, st));
-    CK(cudaMemsetAsync(d.dfirst, 0xFF, 32 * (size_t)kp.ncell, st));
+    CK(cudaMemsetAsync(d.dfirst, 0xFF, 16 * (size_t)kp.ncell, st));
     CK(cudaMemsetAsync(d.affected, 0, (size_t)kp.ncell, st));
     StepArgs a = args(cstep);
     Launch<T>::accumulate_main(d, kp, a, 2, st);
@@ -834,14 +834,14 @@ struct Engine : EngineBase {
 
   int get_distribute(int32_t* counts, int64_t* first) override {
     std::vector<uint32_t> cn((size_t)kp.ncell);
-    std::vector<unsigned long long> fk((size_t)kp.ncell * 4);
+    std::vector<uint32_t> fk((size_t)kp.ncell * 4);
     CK(cudaMemcpy(cn.data(), d.dcnt, cn.size() * 4, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(fk.data(), d.dfirst, fk.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(fk.data(), d.dfirst, fk.size() * 4, cudaMemcpyDeviceToHost));
     for (int64_t c = 0; c < kp.ncell; ++c)
       for (int s = 0; s < 4; ++s) {
         if (counts) counts[4 * c + s] = (int32_t)((cn[(size_t)c] >> (8 * s)) & 255u);
-        unsigned long long key = fk[(size_t)(4 * c + s)];
-        if (first) first[4 * c + s] = key == ~0ull ? -1 : (int64_t)((key >> 31) & 0xFFFFFFFFull);
+        const uint32_t key = fk[(size_t)(4 * c + s)];
+        if (first) first[4 * c + s] = key == 0xFFFFFFFFu ? -1 : (int64_t)(key & 0x7FFFFFFFu);
       }
     return MPCMD_OK;
   }

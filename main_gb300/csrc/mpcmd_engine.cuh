@@ -86,7 +86,7 @@ struct Dev {
   void* acc;               // [ncell_shift] float4 (FP32) or double4 (FP64): n, sum v
   T* rot;                  // [ncell_shift * 6] centre-of-mass velocity and axis
   uint32_t* dcnt;          // [ncell] packed per-species counts (8 bits each)
-  unsigned long long* dfirst;  // [ncell * 4] first member key per species
+  uint32_t* dfirst;        // [ncell * 4] first member key per species (dist_key)
   uint8_t* affected;       // [ncell]
   uint8_t* react_box;      // [lx*ly]
   uint32_t* order_rank;    // [ncell] position of each cell in the sort order

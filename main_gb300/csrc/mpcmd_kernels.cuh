@@ -37,15 +37,18 @@ __device__ __forceinline__ void accum_coll<double>(void* acc, uint32_t key, doub
 // cell cid and keep the smallest ordering key (first member of the list).
 template <typename T>
 __device__ __forceinline__ void accum_dist(const Dev<T>& d, const KParams<T>& kp, uint32_t cid, int sp,
-                                           unsigned long long key) {
+                                           uint32_t key) {
   unsigned int old = atomicAdd(&d.dcnt[cid], 1u << (8 * sp));
   unsigned int before = (old >> (8 * sp)) & 255u;
   if (before + 1u > (unsigned)kp.cell_capacity) atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
   atomicMin(&d.dfirst[4 * (size_t)cid + sp], key);
 }
 
-__device__ __forceinline__ unsigned long long dist_key(int group, uint32_t idx, uint32_t slot1) {
-  return ((unsigned long long)group << 63) | ((unsigned long long)idx << 31) | (unsigned long long)slot1;
+// Ordering key of a species-list member: group (0 outside, 1 inside when the
+// lists put the inside particles last) above the main index (< 2^31).  The
+// smallest key of a cell is its first member; 0xFFFFFFFF is "none".
+__device__ __forceinline__ uint32_t dist_key(int group, uint32_t idx) {
+  return ((uint32_t)group << 31) | idx;
 }
 
 template <typename T>
@@ -485,7 +488,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
         pend_cnt = __popc(peers);
         pend_shift = 8 * sp;
         pend_old = atomicAdd(&d.dcnt[cid], pend_cnt << pend_shift);
-        atomicMin(&d.dfirst[4 * (size_t)cid + sp], dist_key(0, (uint32_t)i, 0));
+        atomicMin(&d.dfirst[4 * (size_t)cid + sp], dist_key(0, (uint32_t)i));
       }
     }
   }
@@ -665,7 +668,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
           bool bulk = kp.exclusion == 1 || !d.sh.nonbulk[j];
           if (bulk)
             accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), fl & FLAG_SPECIES,
-                       dist_key(kp.exclusion == 0 ? 1 : 0, idx, (uint32_t)j + 1u));
+                       dist_key(kp.exclusion == 0 ? 1 : 0, idx));
         }
       }
       if (a.advance && !a.mpc) {
@@ -1013,7 +1016,7 @@ __global__ void __launch_bounds__(TPB) k_accumulate_main(Dev<T> d, KParams<T> kp
       }
       if (bulk)
         accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), f & FLAG_SPECIES,
-                   dist_key(kp.exclusion == 0 && inl ? 1 : 0, (uint32_t)i, 0));
+                   dist_key(kp.exclusion == 0 && inl ? 1 : 0, (uint32_t)i));
     }
   }
 }
@@ -1025,11 +1028,20 @@ void Launch<T>::accumulate_main(const Dev<T>& d, const KParams<T>& kp, const Ste
 }
 
 // ------------------------------------------------------------ per cell ----
-__device__ __forceinline__ void relabel_key(uint8_t* main_flag, uint8_t* shell_flag, unsigned long long key, int code) {
-  uint32_t idx = (uint32_t)((key >> 31) & 0xFFFFFFFFull);
-  uint32_t slot1 = (uint32_t)(key & 0x7FFFFFFFull);
-  if (slot1) shell_flag[slot1 - 1] = (uint8_t)((shell_flag[slot1 - 1] & ~FLAG_SPECIES) | code);
-  else main_flag[idx] = (uint8_t)((main_flag[idx] & ~FLAG_SPECIES) | code);
+// Relabel the list member `key` to species `code`: in the shell buffer when
+// its state lives there (the main cell[] then holds the shell slot), else in
+// the main arrays.
+template <typename T>
+__device__ __forceinline__ void relabel_key(const Dev<T>& d, uint32_t key, int code) {
+  const uint32_t idx = key & 0x7FFFFFFFu;
+  const uint8_t f = d.p.flag[idx];
+  if (f & FLAG_HOME_SHELL) {
+    const uint32_t j = d.p.cell[idx];
+    if (!chk((int64_t)j < d.sh.cap, d.ctr, 120, j)) return;
+    d.sh.flag[j] = (uint8_t)((d.sh.flag[j] & ~FLAG_SPECIES) | code);
+  } else {
+    d.p.flag[idx] = (uint8_t)((f & ~FLAG_SPECIES) | code);
+  }
 }
 
 // Selkov six-channel RKMPC decision for one cell (RMPC_SelkovDimer.f90:132-321)
@@ -1141,7 +1153,7 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
     }
     if ((what & 2) && c < kp.ncell) {
       unsigned int cnt = d.dcnt[c];
-      unsigned long long* fk = d.dfirst + 4 * (size_t)c;
+      uint32_t* fk = d.dfirst + 4 * (size_t)c;
       if (kp.kinetics == 1) {
         int nB = (cnt >> 8) & 255u;
         double u0, u1;
@@ -1158,7 +1170,7 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
             double prob1 = 1.0 - exp(-a1 * kp.tau);
             fire = (0. < u0 && u0 <= prob1);
           }
-          if (fire) relabel_key(d.p.flag, d.sh.flag, fk[1], 0);
+          if (fire && fk[1] != 0xFFFFFFFFu) relabel_key(d, fk[1], 0);
         }
       } else if (kp.kinetics == 2 && !d.affected[c]) {
         const int tgt[7] = {-1, 3, 0, 0, 1, 1, 3};
@@ -1170,12 +1182,12 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
         if (sizeof(T) == 4) ch = selkov_channel_fp32(kp.k, (float)kp.tau, nF, nG, nI, x1, x2);
         if (ch < 0) ch = selkov_channel_fp64(kp.k, kp.tau, nF, nG, nI, x1, x2);
         if (ch > 0) {
-          unsigned long long key = fk[tgt[ch]];
-          if (key != ~0ull) relabel_key(d.p.flag, d.sh.flag, key, code[ch]);
+          const uint32_t key = fk[tgt[ch]];
+          if (key != 0xFFFFFFFFu) relabel_key(d, key, code[ch]);
         }
       }
       d.dcnt[c] = 0u;
-      fk[0] = fk[1] = fk[2] = fk[3] = ~0ull;
+      *reinterpret_cast<uint4*>(fk) = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
       d.affected[c] = 0;
     }
   }
