@@ -136,7 +136,12 @@ int mpcmd_get_cell_rotation(mpcmd_ctx* ctx, double* cm, double* axis, int32_t* c
 int mpcmd_get_distribute(mpcmd_ctx* ctx, int32_t* counts, int64_t* first);
 int mpcmd_get_affected(mpcmd_ctx* ctx, int32_t* affected);
 int mpcmd_get_shift(mpcmd_ctx* ctx, double* shift);
+/* Pairs (particle, sphere) of the shell buffer entries; between collision
+ * steps, inside-list members in free flight (no LJ cutoff reachable before
+ * the next collision rebuild) are kept outside the buffer and listed by
+ * mpcmd_get_inside only. */
 int mpcmd_get_pairs(mpcmd_ctx* ctx, int64_t* n_pairs, int64_t* particle, int32_t* sphere);
+/* The inside list (neighbour_list_mod.f95 inout_particle_list) of the last rebuild. */
 int mpcmd_get_inside(mpcmd_ctx* ctx, int64_t* n_inside, int64_t* idx);
 int mpcmd_get_counters(mpcmd_ctx* ctx, int64_t* counters, int32_t n);
 int mpcmd_reactive_grid_table(mpcmd_ctx* ctx, int32_t* table);

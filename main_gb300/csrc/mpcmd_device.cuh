@@ -4,9 +4,11 @@
 //   cell  u32   packed cell coordinates ix | iy << 10 | iz << 20 (box edges <= 1024)
 //   ox..  T     offset inside the cell, [0, 1)  (T = float in production, double for parity)
 //   vx..  T     velocity
-//   flag  u8    bits 0-1 species code, bit 5 member of the shell ("inside") list of the
-//               last rebuild, bit 6 state lives in the shell buffer (then cell[] holds the
-//               shell slot)
+//   flag  u8    bits 0-1 species code, bit 4 member of the shell ("inside") list that
+//               flies freely until the next collision and is streamed lazily like an
+//               outside particle, bit 5 member of the shell list of the last rebuild whose
+//               state is current, bit 6 state lives in the shell buffer (then cell[] holds
+//               the shell slot)
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -21,6 +23,7 @@ enum Tag : uint32_t {
 };
 
 constexpr uint8_t FLAG_SPECIES = 0x03;
+constexpr uint8_t FLAG_PASSIVE = 0x10;   // shell member in free flight, kept in the main home
 constexpr uint8_t FLAG_INLIST = 0x20;
 constexpr uint8_t FLAG_HOME_SHELL = 0x40;
 constexpr int PAIRMAX = 8;         // spheres one shell particle may interact with

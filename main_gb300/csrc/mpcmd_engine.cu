@@ -107,7 +107,8 @@ std::vector<uint8_t> reactive_table(const mpcmd_config& c) {
 
 int dev_status_to_api(int bits) {
   if (bits & DEV_ERR_CELL_OVERFLOW) return MPCMD_ERR_CELL_OVERFLOW;
-  if (bits & (DEV_ERR_SHELL_OVERFLOW | DEV_ERR_PAIR_OVERFLOW | DEV_ERR_BIN_OVERFLOW)) return MPCMD_ERR_NEIGHBOUR_OVERFLOW;
+  if (bits & (DEV_ERR_SHELL_OVERFLOW | DEV_ERR_PAIR_OVERFLOW | DEV_ERR_BIN_OVERFLOW | DEV_ERR_PASSIVE))
+    return MPCMD_ERR_NEIGHBOUR_OVERFLOW;
   if (bits & DEV_ERR_RATTLE) return MPCMD_ERR_RATTLE;
   if (bits & DEV_ERR_INIT) return MPCMD_ERR_INIT;
   return MPCMD_OK;
@@ -458,7 +459,7 @@ struct Engine : EngineBase {
     double* outs[6] = {x, y, z, vx, vy, vz};
     for (int c = 0; c < 6; ++c) {
       if (!outs[c]) continue;
-      Launch<T>::download_convert(d, kp, d.staging, c, st);
+      Launch<T>::download_convert(d, kp, d.staging, c, time_count, st);
       CK(cudaMemcpyAsync(outs[c], d.staging, sizeof(double) * kp.n, cudaMemcpyDeviceToHost, st));
     }
     if (flag) {
@@ -498,10 +499,18 @@ struct Engine : EngineBase {
   // The rebuild block of evolve_mod.f95:465-564 at step n (lazy streaming by
   // tc, optional sort, lists, time_penetrate).  Synchronises; on return the new
   // shell buffer is current.
-  int do_rebuild(int64_t n, int tc, bool mpc) {
+  // Steps from step m to the next collision step (where a rebuild always
+  // runs and merges the free-flight shell members back).
+  int steps_to_collision(int64_t m) const {
+    return cfg.mpc_every - (int)(m % cfg.mpc_every);
+  }
+
+  int do_rebuild(int64_t n, int tc, bool mpc, bool free_flight = false) {
     StepArgs a = args(n);
     a.tc = tc;
     a.mpc = mpc ? 1 : 0;
+    // free-flight shell members only between collision steps
+    a.horizon = (free_flight && n % cfg.mpc_every != 0) ? steps_to_collision(n) : 0;
     pb(PROF_BINS); Launch<T>::build_bins(d, kp, st); pe();
     bool sort_now = cfg.sort_every > 0 && n % cfg.sort_every == 0;
     if (sort_now) {
@@ -580,7 +589,10 @@ struct Engine : EngineBase {
       if (!advanced) {
         StepArgs a = args(n - 1);
         a.advance = 1;
+        // right after a rebuild the shell can be sorted into free-flight and active members
+        a.horizon = time_count == 0 ? steps_to_collision(n - 1) : 0;
         pb(PROF_SHELL_ADVANCE); Launch<T>::advance(d, kp, a, st); pe();
+        if (a.horizon > 0) std::swap(d.sh, d.sh2);
         pb(PROF_DIMER); Launch<T>::dimer(d, kp, a, 2, w3, cfg.rattle_max_iter, st); pe();
         advanced = true;
       }
@@ -591,7 +603,7 @@ struct Engine : EngineBase {
       if (mpc) draw_shift(n);
       if (rebuild) {
         force_rebuild_step = -1;
-        int r = do_rebuild(n, time_count, mpc);
+        int r = do_rebuild(n, time_count, mpc, true);
         if (r == -1) {
           Counters h;
           if ((r = read_counters(h))) return r;
@@ -613,7 +625,10 @@ struct Engine : EngineBase {
       if (mpc) {
         pb(PROF_CELLS); Launch<T>::cells(d, kp, a, 1 | (kp.kinetics ? 2 : 0), st); pe();
         pb(PROF_ROTATE_MAIN); Launch<T>::rotate_main(d, kp, a, st); pe();
-        pb(PROF_SHELL_ADVANCE); Launch<T>::rotate_shell(d, kp, a, st); pe();
+        StepArgs ar = a;
+        ar.horizon = a.advance ? cfg.mpc_every : 0;   // the rebuild of this step was the last one
+        pb(PROF_SHELL_ADVANCE); Launch<T>::rotate_shell(d, kp, ar, st); pe();
+        if (ar.horizon > 0) std::swap(d.sh, d.sh2);
       }
       advanced = !last;
       cstep = n;
@@ -857,11 +872,19 @@ struct Engine : EngineBase {
     Counters h;
     int r = read_counters(h);
     if (r) return r;
-    *n = h.n_inside;
-    if (idx && h.n_inside) {
+    // the shell buffer, then the free-flight members kept in the main home
+    std::vector<uint8_t> fl((size_t)kp.n);
+    CK(cudaMemcpy(fl.data(), d.p.flag, fl.size(), cudaMemcpyDeviceToHost));
+    int64_t m = h.n_inside;
+    for (size_t i = 0; i < fl.size(); ++i) m += (fl[i] & FLAG_PASSIVE) ? 1 : 0;
+    *n = m;
+    if (idx) {
       std::vector<uint32_t> v(h.n_inside);
-      CK(cudaMemcpy(v.data(), d.sh.idx, v.size() * 4, cudaMemcpyDeviceToHost));
-      for (size_t j = 0; j < v.size(); ++j) idx[j] = v[j];
+      if (h.n_inside) CK(cudaMemcpy(v.data(), d.sh.idx, v.size() * 4, cudaMemcpyDeviceToHost));
+      size_t k = 0;
+      for (; k < v.size(); ++k) idx[k] = v[k];
+      for (size_t i = 0; i < fl.size(); ++i)
+        if (fl[i] & FLAG_PASSIVE) idx[k++] = (int64_t)i;
     }
     return MPCMD_OK;
   }

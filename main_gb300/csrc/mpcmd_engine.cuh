@@ -17,6 +17,7 @@ enum : int {
   DEV_ERR_BIN_OVERFLOW = 1 << 3,
   DEV_ERR_RATTLE = 1 << 4,
   DEV_ERR_INIT = 1 << 5,
+  DEV_ERR_PASSIVE = 1 << 6,   // a free-flight shell member was found inside an LJ cutoff
 };
 
 struct Counters {
@@ -33,6 +34,7 @@ struct Counters {
   int dbg_code;                   // checked builds: first failed bounds check
   int dbg_pad;
   long long dbg_val;
+  unsigned long long vsph;        // bits of the largest sphere speed seen (double)
 };
 
 // Bounds check of the checked build (MPCMD_CHECKED): records the first failing
@@ -112,6 +114,8 @@ struct StepArgs {
   int g_rebuild;       // SMs x resident blocks of k_rebuild, k_force, k_rotate_main
   int g_force;
   int g_rotate;
+  int horizon;         // > 0: steps to the next collision rebuild; shell members that
+                       // cannot reach an LJ cutoff or a wall before it fly freely
   double shift[3];     // collision grid shift of this step
 };
 
@@ -120,13 +124,17 @@ struct Launch {
   static void upload_convert(const Dev<T>& d, const KParams<T>& kp, const double* x, const double* y,
                              const double* z, const double* vx, const double* vy, const double* vz,
                              const int32_t* flag, cudaStream_t st);
-  static void download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, cudaStream_t st);
+  static void download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
+                               cudaStream_t st);
   static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st);
   static void update_srel(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
   static void finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, double skin, cudaStream_t st);
   static void force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  // kick + free flight of the shell; with a.horizon > 0 it also moves the
+  // free-flight members to the main home and compacts the rest into d.sh2
+  // (the caller then swaps d.sh and d.sh2)
   static void advance(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
   static void dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode,
                     double w3, int rattle_max, cudaStream_t st);

@@ -194,23 +194,34 @@ void Launch<T>::upload_convert(const Dev<T>& d, const KParams<T>& kp, const doub
   LAUNCH_COUNT();
 }
 
+// Host view of one component.  A free-flight shell member (FLAG_PASSIVE) is
+// shown at the current step: its stored state is streamed by the tc steps
+// since the last rebuild, as the reference streams its inside particles every
+// step (outside particles stay lazily streamed, as in the reference).
 template <typename T>
-__global__ void k_download(Particles<T> p, KParams<T> kp, double* out, int comp) {
+__global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_box, double* out, int comp, int tc) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
     uint32_t c = p.cell[i];
+    T ox = p.ox[i], oy = p.oy[i], oz = p.oz[i];
+    T vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
+    if ((p.flag[i] & FLAG_PASSIVE) && tc > 0) {
+      uint8_t ff = p.flag[i];
+      stream_one(kp, react_box, c, ox, oy, oz, vx, vy, vz, ff, true, tc);
+    }
     double v;
-    if (comp == 0) v = (double)cell_x(c) + (double)p.ox[i];
-    else if (comp == 1) v = (double)cell_y(c) + (double)p.oy[i];
-    else if (comp == 2) v = (double)cell_z(c) + (double)p.oz[i];
-    else v = (double)(comp == 3 ? p.vx : comp == 4 ? p.vy : p.vz)[i];
+    if (comp == 0) v = (double)cell_x(c) + (double)ox;
+    else if (comp == 1) v = (double)cell_y(c) + (double)oy;
+    else if (comp == 2) v = (double)cell_z(c) + (double)oz;
+    else v = (double)(comp == 3 ? vx : comp == 4 ? vy : vz);
     out[i] = v;
   }
 }
 
 template <typename T>
-void Launch<T>::download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, cudaStream_t st) {
-  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, out, comp);
+void Launch<T>::download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
+                                 cudaStream_t st) {
+  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, comp, tc);
   LAUNCH_COUNT();
 }
 
@@ -288,6 +299,10 @@ __global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn) {
   const int s = blockIdx.x;
   if (s >= kp.ns) return;
   const double R = (s & 1) ? Rn : Rc;
+  if (threadIdx.x == 0) {
+    const double* V = d.dvel + 3 * s;
+    atomicMax(&d.ctr->vsph, ord_bits(sqrt(V[0] * V[0] + V[1] * V[1] + V[2] * V[2])));
+  }
   int lo[3], hi[3];
   bool wr[3];
   const int L[3] = {kp.lx, kp.ly, kp.lz};
@@ -338,6 +353,37 @@ void Launch<T>::build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t s
 
 __device__ __forceinline__ int bin_of(int lx, int ly, int nbx, int nby, uint32_t cell) {
   return cell_x(cell) / BIN_EDGE + nbx * (cell_y(cell) / BIN_EDGE + nby * (cell_z(cell) / BIN_EDGE));
+}
+
+// Free-flight test of a shell member.  The reference integrates every member
+// of its inside list each MD step (evolve_mod.f95:225-316).  A member that,
+// at its constant velocity, cannot come within an LJ cutoff of a listed sphere
+// (the spheres moving at most vs) before the next collision rebuild, cannot
+// hit a wall and cannot reach the displacement criterion gets no force and no
+// kick until then, so the engine streams it lazily instead (same positions up
+// to rounding).  min_gap is the smallest distance beyond the cutoff over its
+// listed spheres.
+template <typename T>
+__device__ __forceinline__ bool free_flight_ok(const KParams<T>& kp, uint32_t cell, T oz, T vx, T vy, T vz, T msd,
+                                               T min_gap, int horizon, T vs) {
+  const T v2 = vx * vx + vy * vy + vz * vz;
+  const T t = kp.dt * (T)horizon;
+  const T reach = (sqrt(v2) + vs) * t + (T)0.1;
+  if (!(min_gap > reach)) return false;
+  if (!(msd + (T)horizon * v2 * (kp.dt * kp.dt) < kp.msd_thr)) return false;
+  if (kp.geometry == 0) {
+    const T z0 = (T)cell_z(cell) + oz, z1 = z0 + vz * t;
+    const T lo = (T)0.05, hi = (T)kp.lz - (T)0.05;
+    if (!(z0 > lo && z0 < hi && z1 > lo && z1 < hi)) return false;
+  }
+  return true;
+}
+
+// Bound on the sphere speeds over the next collision period: twice the
+// largest speed seen so far plus a margin.
+template <typename T>
+__device__ __forceinline__ T sphere_speed_bound(const Counters* c) {
+  return (T)(2.0 * __longlong_as_double((long long)c->vsph) + 0.05);
 }
 
 // ------------------------------------------------------------- rebuild ----
@@ -408,6 +454,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
         // candidate spheres of this particle's coarse bin
         int np = 0;
         bool nonbulk = false;
+        T min_gap = (T)1e30;
         uint16_t sph[PAIRMAX];
         if (kp.ns > 0) {
           int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
@@ -425,12 +472,22 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
               if (np < PAIRMAX) sph[np] = (uint16_t)s;
               np++;
               if (d2 <= kp.cut2[s & 1]) nonbulk = true;
+              if (a.horizon > 0) {
+                const T gap = sqrt(d2) - sqrt(kp.cut2[s & 1]);
+                min_gap = gap < min_gap ? gap : min_gap;
+              }
             }
           }
         }
         if (np > PAIRMAX) { atomicOr(&d.ctr->status, DEV_ERR_PAIR_OVERFLOW); np = PAIRMAX; }
+        // a free-flight member must not have entered a cutoff since it was classified
+        if ((f & FLAG_PASSIVE) && nonbulk) atomicOr(&d.ctr->status, DEV_ERR_PASSIVE);
+        const bool passive = np > 0 && a.horizon > 0 && !a.mpc &&
+                             free_flight_ok(kp, cell, oz, vx, vy, vz, (T)0, min_gap, a.horizon,
+                                            sphere_speed_bound<T>(d.ctr));
+        const uint8_t nf = passive ? (uint8_t)(sp | FLAG_PASSIVE) : sp;
         bool placed = false;
-        if (np > 0) {
+        if (np > 0 && !passive) {
           cg::coalesced_group g = cg::coalesced_threads();
           unsigned int bslot = 0;
           if (g.thread_rank() == 0) bslot = atomicAdd(&d.ctr->n_inside_new, g.size());
@@ -463,7 +520,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
           if (wr_cell) d.p.cell[i] = cell;
           if (wr_pos) { d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz; }
           if (wr_vel) { d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz; }
-          if (wr_flag) d.p.flag[i] = sp;
+          if (wr_all || nf != f) d.p.flag[i] = nf;
           if (a.mpc) {
             uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
             d.skey[i] = key;
@@ -708,11 +765,20 @@ void Launch<T>::force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, 
 // First half kick with the stored pair forces and free flight of the shell
 // particles (evolve_mod.f95:225-316), used after a collision step or at the
 // start of a run call; with rotate set it first applies the collision.
+// With a.advance and a.horizon > 0 (right after a rebuild) it also sorts the
+// shell: members that pass free_flight_ok move to the main home with
+// FLAG_PASSIVE and their state of this step (they are streamed lazily from
+// here), the others are streamed and packed into d.sh2, which the caller makes
+// the current shell.
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, StepArgs a, int rotate) {
-  if (d.ctr->abort_step) return;
+  const bool sort_shell = a.advance && a.horizon > 0;
+  // (no displacement abort can be pending where the shell is sorted, and the
+  // sorted buffer must be produced whatever happens)
+  if (d.ctr->abort_step && !sort_shell) return;
   const unsigned int nin = d.ctr->n_inside;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const T vs = sphere_speed_bound<T>(d.ctr);
   T msdmax = (T)0;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
     T vx = d.sh.vx[j], vy = d.sh.vy[j], vz = d.sh.vz[j];
@@ -730,6 +796,53 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
         size_t b = ((size_t)j * PAIRMAX + q) * 3;
         vx = vx + h2 * d.sh.pf[b]; vy = vy + h2 * d.sh.pf[b + 1]; vz = vz + h2 * d.sh.pf[b + 2];
       }
+      if (sort_shell) {
+        const uint4 packed = *reinterpret_cast<const uint4*>(d.sh.sph + (size_t)j * PAIRMAX);
+        const uint16_t ids[PAIRMAX] = {
+            (uint16_t)(packed.x & 0xFFFFu), (uint16_t)(packed.x >> 16), (uint16_t)(packed.y & 0xFFFFu),
+            (uint16_t)(packed.y >> 16), (uint16_t)(packed.z & 0xFFFFu), (uint16_t)(packed.z >> 16),
+            (uint16_t)(packed.w & 0xFFFFu), (uint16_t)(packed.w >> 16)};
+        T min_gap = (T)1e30;
+        for (int q = 0; q < np; ++q) {
+          const int s = ids[q];
+          if (!chk(s < kp.ns, d.ctr, 121, s)) { min_gap = (T)-1; break; }
+          T dx, dy, dz;
+          const T d2 = sep2(kp, cell, ox, oy, oz, d.srel[s], dx, dy, dz);
+          const T gap = sqrt(d2) - sqrt(kp.cut2[s & 1]);
+          min_gap = gap < min_gap ? gap : min_gap;
+        }
+        const uint32_t idx = d.sh.idx[j];
+        const T msd_now = d.sh.msd[j];
+        if (free_flight_ok(kp, cell, oz, vx, vy, vz, msd_now, min_gap, a.horizon, vs)) {
+          // state of this step into the main home; no force acts before the
+          // next rebuild, which streams it with the outside particles
+          d.p.cell[idx] = cell;
+          d.p.ox[idx] = ox; d.p.oy[idx] = oy; d.p.oz[idx] = oz;
+          d.p.vx[idx] = vx; d.p.vy[idx] = vy; d.p.vz[idx] = vz;
+          d.p.flag[idx] = (uint8_t)((fl & FLAG_SPECIES) | FLAG_PASSIVE);
+          continue;
+        }
+        stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
+        const T msd = msd_now + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
+        msdmax = msd > msdmax ? msd : msdmax;
+        cg::coalesced_group g = cg::coalesced_threads();
+        unsigned int bslot = 0;
+        if (g.thread_rank() == 0) bslot = atomicAdd(&d.ctr->n_inside_new, g.size());
+        bslot = g.shfl(bslot, 0);
+        const unsigned int k = bslot + g.thread_rank();
+        if ((int64_t)k >= d.sh2.cap) { atomicOr(&d.ctr->status, DEV_ERR_SHELL_OVERFLOW); continue; }
+        d.sh2.idx[k] = idx;
+        d.sh2.cell[k] = cell;
+        d.sh2.ox[k] = ox; d.sh2.oy[k] = oy; d.sh2.oz[k] = oz;
+        d.sh2.vx[k] = vx; d.sh2.vy[k] = vy; d.sh2.vz[k] = vz;
+        d.sh2.msd[k] = msd;
+        d.sh2.flag[k] = fl;
+        d.sh2.nonbulk[k] = d.sh.nonbulk[j];
+        d.sh2.np[k] = (uint8_t)np;
+        *reinterpret_cast<uint4*>(d.sh2.sph + (size_t)k * PAIRMAX) = packed;
+        d.p.cell[idx] = k;
+        continue;
+      }
       stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
       T msd = d.sh.msd[j] + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
       d.sh.msd[j] = msd;
@@ -743,16 +856,33 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
   if (a.advance) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], (double)msdmax);
 }
 
+// Publish the shell packed by k_shell_advance.
+template <typename T>
+__global__ void k_shell_commit(Counters* c, int64_t cap) {
+  unsigned int m = c->n_inside_new;
+  if ((int64_t)m > cap) m = (unsigned int)cap;
+  c->n_inside = m;
+  c->n_inside_new = 0u;
+}
+
 template <typename T>
 void Launch<T>::advance(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
   k_shell_advance<T><<<a.grid, TPB, 0, st>>>(d, kp, a, 0);
   LAUNCH_COUNT();
+  if (a.advance && a.horizon > 0) {
+    k_shell_commit<T><<<1, 1, 0, st>>>(d.ctr, d.sh2.cap);
+    LAUNCH_COUNT();
+  }
 }
 
 template <typename T>
 void Launch<T>::rotate_shell(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
   k_shell_advance<T><<<a.grid, TPB, 0, st>>>(d, kp, a, 1);
   LAUNCH_COUNT();
+  if (a.advance && a.horizon > 0) {
+    k_shell_commit<T><<<1, 1, 0, st>>>(d.ctr, d.sh2.cap);
+    LAUNCH_COUNT();
+  }
 }
 
 // ---------------------------------------------------------------- dimers ----
