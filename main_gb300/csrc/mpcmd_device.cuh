@@ -4,7 +4,9 @@
 //   cell  u32   packed cell coordinates ix | iy << 10 | iz << 20 (box edges <= 1024)
 //   ox..  T     offset inside the cell, [0, 1)  (T = float in production, double for parity)
 //   vx..  T     velocity
-//   flag  u8    bits 0-1 species code, bit 4 member of the shell ("inside") list that
+//   flag  u8    bits 0-1 species code, bit 3 state written at the last rebuild (else at
+//               the last full pass: rebuilds between collision steps leave far particles
+//               unwritten and their lazy stream deferred), bit 4 member of the shell ("inside") list that
 //               flies freely until the next collision and is streamed lazily like an
 //               outside particle, bit 5 member of the shell list of the last rebuild whose
 //               state is current, bit 6 state lives in the shell buffer (then cell[] holds
@@ -23,6 +25,7 @@ enum Tag : uint32_t {
 };
 
 constexpr uint8_t FLAG_SPECIES = 0x03;
+constexpr uint8_t FLAG_FRESH = 0x08;     // main-home state is at the last rebuild, not the last full pass
 constexpr uint8_t FLAG_PASSIVE = 0x10;   // shell member in free flight, kept in the main home
 constexpr uint8_t FLAG_INLIST = 0x20;
 constexpr uint8_t FLAG_HOME_SHELL = 0x40;

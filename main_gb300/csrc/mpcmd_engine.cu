@@ -175,6 +175,7 @@ struct Engine : EngineBase {
   int64_t cstep = 0;
   int time_count = 0, time_penetrate = 0;
   int64_t last_rebuild = 0;
+  int64_t last_full = 0;   // step of the last rebuild that wrote every particle
   int64_t force_rebuild_step = -1;
   bool prepared = false, home_shell = false, advanced = false;
   double w3 = 1.0;
@@ -402,6 +403,7 @@ struct Engine : EngineBase {
     cstep = c;
     time_count = tc;
     last_rebuild = c - tc;
+    last_full = last_rebuild;
     return MPCMD_OK;
   }
 
@@ -459,7 +461,7 @@ struct Engine : EngineBase {
     double* outs[6] = {x, y, z, vx, vy, vz};
     for (int c = 0; c < 6; ++c) {
       if (!outs[c]) continue;
-      Launch<T>::download_convert(d, kp, d.staging, c, time_count, st);
+      Launch<T>::download_convert(d, kp, d.staging, c, time_count, (int)(last_rebuild - last_full), st);
       CK(cudaMemcpyAsync(outs[c], d.staging, sizeof(double) * kp.n, cudaMemcpyDeviceToHost, st));
     }
     if (flag) {
@@ -508,18 +510,24 @@ struct Engine : EngineBase {
   int do_rebuild(int64_t n, int tc, bool mpc, bool free_flight = false) {
     StepArgs a = args(n);
     a.tc = tc;
+    a.tc_full = (int)(n - last_full);
     a.mpc = mpc ? 1 : 0;
-    // free-flight shell members only between collision steps
-    a.horizon = (free_flight && n % cfg.mpc_every != 0) ? steps_to_collision(n) : 0;
+    const bool collision_step = n % cfg.mpc_every == 0;
+    // free-flight shell members and deferred far particles only between collision steps
+    a.horizon = (free_flight && !collision_step) ? steps_to_collision(n) : 0;
+    a.full = (!free_flight || collision_step) ? 1 : 0;
     pb(PROF_BINS); Launch<T>::build_bins(d, kp, st); pe();
     bool sort_now = cfg.sort_every > 0 && n % cfg.sort_every == 0;
     if (sort_now) {
       StepArgs m = a;
       m.merge_only = 1;
       m.mpc = 0;
+      m.full = 1;
       pb(PROF_REBUILD); Launch<T>::rebuild(d, kp, m, st); pe();
       pb(PROF_SORT); Launch<T>::sort(d, kp, st); pe();
       a.tc = 0;
+      a.tc_full = 0;
+      a.full = 1;
     }
     pb(PROF_REBUILD); Launch<T>::rebuild(d, kp, a, st); pe();
     pb(PROF_FINALIZE); Launch<T>::finalize_rebuild(d, kp, a, cfg.skin, st); pe();
@@ -533,6 +541,7 @@ struct Engine : EngineBase {
     time_penetrate = h.time_penetrate;
     time_count = 0;
     last_rebuild = n;
+    if (a.full) last_full = n;
     home_shell = true;
     prepared = true;
     return MPCMD_OK;
@@ -549,6 +558,7 @@ struct Engine : EngineBase {
     }
     Launch<T>::build_bins(d, kp, st);
     StepArgs a = args(cstep);
+    a.full = 1;
     Launch<T>::rebuild(d, kp, a, st);
     Launch<T>::finalize_rebuild(d, kp, a, cfg.skin, st);
     Counters h;
@@ -560,6 +570,7 @@ struct Engine : EngineBase {
     time_penetrate = h.time_penetrate;
     time_count = 0;
     last_rebuild = cstep;
+    last_full = cstep;
     home_shell = true;
     prepared = true;
     return MPCMD_OK;
@@ -1030,6 +1041,7 @@ int Engine<T>::restore(const char* path) {
   cstep = h.cstep;
   time_count = h.time_count;
   last_rebuild = cstep - time_count;
+  last_full = last_rebuild;
   return MPCMD_OK;
 }
 

@@ -105,7 +105,9 @@ struct Dev {
 // Step-level launch arguments.
 struct StepArgs {
   uint32_t step;       // cstep of the step being executed
-  int tc;              // time_count (lazy streaming factor)
+  int tc;              // time_count: steps since the last rebuild
+  int tc_full;         // steps since the last full pass (lag of deferred main-home states)
+  int full;            // rebuild pass writes every particle (collision steps, sorts, prepare)
   int mpc;             // this step ends with a collision
   int advance;         // fuse kick1 + stream of the next step
   int rebuilt;         // a rebuild ran in this step
@@ -125,7 +127,7 @@ struct Launch {
                              const double* z, const double* vx, const double* vy, const double* vz,
                              const int32_t* flag, cudaStream_t st);
   static void download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
-                               cudaStream_t st);
+                               int tc_defer, cudaStream_t st);
   static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st);
   static void update_srel(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);

@@ -194,20 +194,26 @@ void Launch<T>::upload_convert(const Dev<T>& d, const KParams<T>& kp, const doub
   LAUNCH_COUNT();
 }
 
-// Host view of one component.  A free-flight shell member (FLAG_PASSIVE) is
-// shown at the current step: its stored state is streamed by the tc steps
-// since the last rebuild, as the reference streams its inside particles every
-// step (outside particles stay lazily streamed, as in the reference).
+// Host view of one component, as the reference holds it: inside-list
+// members at the current step, outside particles at the last rebuild (lazy
+// streaming).  A free-flight member (FLAG_PASSIVE) is streamed by the tc steps
+// since the last rebuild; a deferred outside state (written at the last full
+// pass) by the tc_defer steps from that pass to the last rebuild.
 template <typename T>
-__global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_box, double* out, int comp, int tc) {
+__global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_box, double* out, int comp, int tc,
+                           int tc_defer) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
     uint32_t c = p.cell[i];
     T ox = p.ox[i], oy = p.oy[i], oz = p.oz[i];
     T vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
-    if ((p.flag[i] & FLAG_PASSIVE) && tc > 0) {
-      uint8_t ff = p.flag[i];
-      stream_one(kp, react_box, c, ox, oy, oz, vx, vy, vz, ff, true, tc);
+    const uint8_t f = p.flag[i];
+    int lag = 0;
+    if (f & FLAG_PASSIVE) lag = tc;
+    else if (!(f & (FLAG_INLIST | FLAG_FRESH | FLAG_HOME_SHELL))) lag = tc_defer;
+    if (lag > 0) {
+      uint8_t ff = f;
+      stream_one(kp, react_box, c, ox, oy, oz, vx, vy, vz, ff, true, lag);
     }
     double v;
     if (comp == 0) v = (double)cell_x(c) + (double)ox;
@@ -220,8 +226,8 @@ __global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_b
 
 template <typename T>
 void Launch<T>::download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
-                                 cudaStream_t st) {
-  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, comp, tc);
+                                 int tc_defer, cudaStream_t st) {
+  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, comp, tc, tc_defer);
   LAUNCH_COUNT();
 }
 
@@ -417,7 +423,12 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
       const uint32_t cell0 = cell;
       const T vx0 = vx, vy0 = vy, vz0 = vz;
       const bool from_shell = (f & FLAG_HOME_SHELL) != 0;
-      const bool streamed = !from_shell && !(f & FLAG_INLIST) && a.tc > 0;
+      // lag of a main-home state: written at the last rebuild (fresh or free
+      // flight) or at the last full pass (deferred); a flushed shell state is current
+      int lag = 0;
+      if (!from_shell && !(f & FLAG_INLIST)) lag = (f & (FLAG_FRESH | FLAG_PASSIVE)) ? a.tc : a.tc_full;
+      const bool deferred = !from_shell && !(f & (FLAG_INLIST | FLAG_FRESH | FLAG_PASSIVE));
+      const bool streamed = lag > 0;
       bool skip = false;
       if (f & FLAG_HOME_SHELL) {
         uint32_t j = cell;
@@ -428,9 +439,9 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
         sp = d.sh.flag[j] & FLAG_SPECIES;
       } else {
         sp = f & FLAG_SPECIES;
-        if (!(f & FLAG_INLIST) && a.tc > 0) {
+        if (streamed) {
           uint8_t ff = sp;
-          stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, ff, true, a.tc);
+          stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, ff, true, lag);
           sp = ff & FLAG_SPECIES;
         }
       }
@@ -516,11 +527,18 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
             placed = true;
           }
         }
-        if (!placed) {
+        // A rebuild between full passes leaves a deferred outside particle
+        // unwritten (its lazy stream waits for the next full pass) unless its
+        // flight hit a wall; everything else it writes is marked fresh.
+        const bool keep = !placed && !a.full && deferred && !passive && !wr_vel && sp == (f & FLAG_SPECIES);
+        if (!placed && !keep) {
+          const uint8_t nf2 = (a.full || passive) ? nf : (uint8_t)(nf | FLAG_FRESH);
           if (wr_cell) d.p.cell[i] = cell;
           if (wr_pos) { d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz; }
           if (wr_vel) { d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz; }
-          if (wr_all || nf != f) d.p.flag[i] = nf;
+          if (wr_all || nf2 != f) d.p.flag[i] = nf2;
+        }
+        if (!placed) {
           if (a.mpc) {
             uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
             d.skey[i] = key;
