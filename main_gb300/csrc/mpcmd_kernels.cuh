@@ -409,17 +409,33 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   // warp-aligned grid-stride loop: the distribute counts are aggregated over
   // the lanes of a warp that fall in the same cell
   unsigned int pend_old = 0, pend_shift = 0, pend_cnt = 0;
+  // The main-array state of the next iteration is loaded before the current
+  // one is processed, so that two iterations' loads are in flight.
+  const int64_t first = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31) + lane;
+  uint8_t pf_f = 0;
+  uint32_t pf_cell = 0;
+  T pf_ox = 0, pf_oy = 0, pf_oz = 0, pf_vx = 0, pf_vy = 0, pf_vz = 0;
+  if (first < kp.n) {
+    pf_f = d.p.flag[first]; pf_cell = d.p.cell[first];
+    pf_ox = d.p.ox[first]; pf_oy = d.p.oy[first]; pf_oz = d.p.oz[first];
+    pf_vx = d.p.vx[first]; pf_vy = d.p.vy[first]; pf_vz = d.p.vz[first];
+  }
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < kp.n; base += stride) {
     const int64_t i = base + lane;
     bool dist = false;
     uint32_t cid = 0;
     uint8_t sp = 0;
+    uint8_t f = pf_f;
+    uint32_t cell = pf_cell;
+    T ox = pf_ox, oy = pf_oy, oz = pf_oz;
+    T vx = pf_vx, vy = pf_vy, vz = pf_vz;
+    const int64_t inext = i + stride;
+    if (inext < kp.n) {
+      pf_f = d.p.flag[inext]; pf_cell = d.p.cell[inext];
+      pf_ox = d.p.ox[inext]; pf_oy = d.p.oy[inext]; pf_oz = d.p.oz[inext];
+      pf_vx = d.p.vx[inext]; pf_vy = d.p.vy[inext]; pf_vz = d.p.vz[inext];
+    }
     if (i < kp.n) {
-      // all main-array loads issue together (no dependence on the flag)
-      uint8_t f = d.p.flag[i];
-      uint32_t cell = d.p.cell[i];
-      T ox = d.p.ox[i], oy = d.p.oy[i], oz = d.p.oz[i];
-      T vx = d.p.vx[i], vy = d.p.vy[i], vz = d.p.vz[i];
       const uint32_t cell0 = cell;
       const T vx0 = vx, vy0 = vy, vz0 = vz;
       const bool from_shell = (f & FLAG_HOME_SHELL) != 0;
