@@ -516,7 +516,7 @@ struct Engine : EngineBase {
     // free-flight shell members and deferred far particles only between collision steps
     a.horizon = (free_flight && !collision_step) ? steps_to_collision(n) : 0;
     a.full = (!free_flight || collision_step) ? 1 : 0;
-    pb(PROF_BINS); Launch<T>::build_bins(d, kp, st); pe();
+    pb(PROF_BINS); Launch<T>::build_bins(d, kp, a.full ? 0 : a.tc_full, st); pe();
     bool sort_now = cfg.sort_every > 0 && n % cfg.sort_every == 0;
     if (sort_now) {
       StepArgs m = a;
@@ -556,7 +556,7 @@ struct Engine : EngineBase {
     if (cfg.sort_every > 0 && cstep % cfg.sort_every == 0) {
       Launch<T>::sort(d, kp, st);
     }
-    Launch<T>::build_bins(d, kp, st);
+    Launch<T>::build_bins(d, kp, 0, st);
     StepArgs a = args(cstep);
     a.full = 1;
     Launch<T>::rebuild(d, kp, a, st);
@@ -675,7 +675,7 @@ struct Engine : EngineBase {
   int distribute_stage() override {
     if (advanced) return MPCMD_ERR_STATE;
     flush_shell();
-    if (kp.ns > 0) Launch<T>::build_bins(d, kp, st);
+    if (kp.ns > 0) Launch<T>::build_bins(d, kp, 0, st);
     CK(cudaMemsetAsync(d.dcnt, 0, 4 * (size_t)kp.ncell, st));
     CK(cudaMemsetAsync(d.dfirst, 0xFF, 16 * (size_t)kp.ncell, st));
     CK(cudaMemsetAsync(d.affected, 0, (size_t)kp.ncell, st));
@@ -793,7 +793,7 @@ struct Engine : EngineBase {
       Launch<T>::update_srel(d, kp, st);
     }
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
-    Launch<T>::build_bins(d, kp, st);
+    Launch<T>::build_bins(d, kp, 0, st);
     Launch<T>::init_solvent(d, kp, bounds, cfg.kT, cfg.mass, st);
     CK(cudaStreamSynchronize(st));
     prepared = false; home_shell = false; advanced = false; n_inside = 0;

@@ -35,6 +35,8 @@ struct Counters {
   int dbg_pad;
   long long dbg_val;
   unsigned long long vsph;        // bits of the largest sphere speed seen (double)
+  unsigned long long vlast;       // bits of max v^2 over all particles at the last rebuild
+  unsigned long long vpost;       // bits of max v^2 of the outside particles after the last collision
 };
 
 // Bounds check of the checked build (MPCMD_CHECKED): records the first failing
@@ -130,7 +132,9 @@ struct Launch {
                                int tc_defer, cudaStream_t st);
   static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st);
   static void update_srel(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
-  static void build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
+  // tc_defer > 0: bins also reach every sphere that a deferred particle,
+  // stored tc_defer steps ago, can be near now (for the rebuild fast path)
+  static void build_bins(const Dev<T>& d, const KParams<T>& kp, int tc_defer, cudaStream_t st);
   static void rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
   static void finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, double skin, cudaStream_t st);
   static void force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);

@@ -301,10 +301,19 @@ __device__ __forceinline__ bool bin_first(int c, int lo, int L, bool wraps, int&
 }
 
 template <typename T>
-__global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn) {
+__global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn, int tc_defer) {
   const int s = blockIdx.x;
   if (s >= kp.ns) return;
-  const double R = (s & 1) ? Rn : Rc;
+  double R = (s & 1) ? Rn : Rc;
+  if (tc_defer > 0) {
+    // the farthest a deferred particle can be from its stored position: its
+    // speed is bounded by the last rebuild's maximum or, after a collision,
+    // by the maximum over the rotated outside particles; plus one cell for
+    // the in-cell offset
+    const double v2 = fmax(__longlong_as_double((long long)d.ctr->vlast),
+                           __longlong_as_double((long long)d.ctr->vpost));
+    R += sqrt(v2) * kp.dtd * (double)tc_defer + 1.0;
+  }
   if (threadIdx.x == 0) {
     const double* V = d.dvel + 3 * s;
     atomicMax(&d.ctr->vsph, ord_bits(sqrt(V[0] * V[0] + V[1] * V[1] + V[2] * V[2])));
@@ -347,12 +356,12 @@ __global__ void k_bins_sort(Dev<T> d, int nbins) {
 }
 
 template <typename T>
-void Launch<T>::build_bins(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
+void Launch<T>::build_bins(const Dev<T>& d, const KParams<T>& kp, int tc_defer, cudaStream_t st) {
   int nbins = kp.nbx * kp.nby * kp.nbz;
   cudaMemsetAsync(d.bin_cnt, 0, sizeof(uint32_t) * nbins, st);
   if (kp.ns == 0) return;
   double Rc = sqrt((double)kp.full2[0]) + 1e-6, Rn = sqrt((double)kp.full2[1]) + 1e-6;
-  k_bins_fill<T><<<kp.ns, 128, 0, st>>>(d, kp, Rc, Rn);
+  k_bins_fill<T><<<kp.ns, 128, 0, st>>>(d, kp, Rc, Rn, tc_defer);
   k_bins_sort<T><<<(nbins + 255) / 256, 256, 0, st>>>(d, nbins);
   LAUNCH_COUNT(); LAUNCH_COUNT();
 }
@@ -446,6 +455,19 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
       const bool deferred = !from_shell && !(f & (FLAG_INLIST | FLAG_FRESH | FLAG_PASSIVE));
       const bool streamed = lag > 0;
       bool skip = false;
+      // Fast path of a rebuild between full passes: a deferred particle whose
+      // stored bin reaches no sphere (the bins are widened by the largest
+      // flight since the full pass) and whose flight hits no wall can be
+      // neither in a list nor written; only its speed counts.
+      if (!a.full && deferred) {
+        const bool nosph = kp.ns == 0 || d.bin_cnt[bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell)] == 0u;
+        bool nowall = true;
+        if (kp.geometry == 0) {
+          const T z = (T)cell_z(cell) + oz + vz * (kp.dt * (T)a.tc_full);
+          nowall = z > (T)1e-3 && z < (T)kp.lz - (T)1e-3;
+        }
+        skip = nosph && nowall;
+      }
       if (f & FLAG_HOME_SHELL) {
         uint32_t j = cell;
         if (!chk((int64_t)j < d.sh.cap, d.ctr, 109, j)) { skip = true; j = 0; }
@@ -455,7 +477,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
         sp = d.sh.flag[j] & FLAG_SPECIES;
       } else {
         sp = f & FLAG_SPECIES;
-        if (streamed) {
+        if (streamed && !skip) {
           uint8_t ff = sp;
           stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, ff, true, lag);
           sp = ff & FLAG_SPECIES;
@@ -599,6 +621,8 @@ __global__ void k_finalize(Dev<T> d, KParams<T> kp, StepArgs a, double skin) {
   if (d.ctr->abort_step) return;
   double maxt = __longlong_as_double((long long)d.ctr->maxv2);
   d.ctr->time_penetrate = (int)floor((0.5 * skin / sqrt(maxt)) / kp.dtd);
+  d.ctr->vlast = d.ctr->maxv2;
+  if (a.mpc) d.ctr->vpost = 0ull;
   d.ctr->maxv2 = 0ull;
   d.ctr->maxmsd[0] = 0ull;
   d.ctr->maxmsd[1] = 0ull;
@@ -1369,6 +1393,7 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
   // two particles per thread and iteration: all loads and both table gathers
   // are issued before the first store
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  T vmax2 = (T)0;   // speed bound of the outside particles until the next collision
   for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < kp.n; i0 += 2 * stride) {
     const int64_t i1 = i0 + stride;
     const bool h1 = i1 < kp.n;
@@ -1389,12 +1414,17 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
     if (r0) {
       rotate_v(kp, t0, vx0, vy0, vz0);
       d.p.vx[i0] = vx0; d.p.vy[i0] = vy0; d.p.vz[i0] = vz0;
+      const T w = vx0 * vx0 + vy0 * vy0 + vz0 * vz0;
+      vmax2 = w > vmax2 ? w : vmax2;
     }
     if (r1) {
       rotate_v(kp, t1, vx1, vy1, vz1);
       d.p.vx[i1] = vx1; d.p.vy[i1] = vy1; d.p.vz[i1] = vz1;
+      const T w = vx1 * vx1 + vy1 * vy1 + vz1 * vz1;
+      vmax2 = w > vmax2 ? w : vmax2;
     }
   }
+  block_max_to<T>(&d.ctr->vpost, (double)vmax2);
 }
 
 template <typename T>
