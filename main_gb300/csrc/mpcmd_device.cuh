@@ -134,6 +134,9 @@ struct KParams {
   float mot_cut2f[3];
   double em, ew, rwc, rwn;
   double mc, mn, dcn;
+  // dimer constants, computed once on the host with the kernel's expressions
+  double hIMc, hIMn, IIM;          // (dt/2)/Mc, (dt/2)/Mn, 1/(1/Mc + 1/Mn)
+  double iMc, iMn, iD2, iMcdt, iMndt;   // 1/Mc, 1/Mn, 1/Dcn^2, 1/(Mc dt), 1/(Mn dt)
   T cut2_strict[2];      // (R * 2^(1/6))^2 for the initial placement test
 };
 

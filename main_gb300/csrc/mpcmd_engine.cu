@@ -327,6 +327,10 @@ struct Engine : EngineBase {
     }
     kp.em = c.em; kp.ew = c.ew; kp.rwc = c.rw + c.rc; kp.rwn = c.rw + c.rn;
     kp.mc = c.mc; kp.mn = c.mn; kp.dcn = c.dcn;
+    kp.hIMc = (0.5 * c.md_dt) / c.mc; kp.hIMn = (0.5 * c.md_dt) / c.mn;
+    kp.IIM = 1.0 / ((1.0 / c.mc) + (1.0 / c.mn));
+    kp.iMc = 1.0 / c.mc; kp.iMn = 1.0 / c.mn; kp.iD2 = 1.0 / (c.dcn * c.dcn);
+    kp.iMcdt = 1.0 / (c.mc * c.md_dt); kp.iMndt = 1.0 / (c.mn * c.md_dt);
     w3 = std::pow(3.0, (double)(1.0f / 6.0f));
 
     // shell capacity from the sphere shells

@@ -993,10 +993,8 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
   if (k >= kp.nd) return;
   constexpr bool fast = sizeof(T) == 4;
   const double dt = kp.dtd, Mc = kp.mc, Mn = kp.mn, Dcn = kp.dcn;
-  const double hIMc = (0.5 * dt) / Mc, hIMn = (0.5 * dt) / Mn;
-  const double IIM = 1.0 / ((1.0 / Mc) + (1.0 / Mn));
-  const double iMc = 1.0 / Mc, iMn = 1.0 / Mn, iD2 = 1.0 / (Dcn * Dcn);
-  const double iMcdt = 1.0 / (Mc * dt), iMndt = 1.0 / (Mn * dt);
+  const double hIMc = kp.hIMc, hIMn = kp.hIMn, IIM = kp.IIM;
+  const double iMc = kp.iMc, iMn = kp.iMn, iD2 = kp.iD2, iMcdt = kp.iMcdt, iMndt = kp.iMndt;
   const bool per = kp.geometry == 1;
   const int nwrap = per ? 3 : 2;
   const int s1 = 2 * k, s2 = 2 * k + 1;
