@@ -178,6 +178,8 @@ struct Engine : EngineBase {
   int64_t last_full = 0;   // step of the last rebuild that wrote every particle
   int64_t force_rebuild_step = -1;
   bool prepared = false, home_shell = false, advanced = false;
+  // the watch list of the last collision is valid (no full pass or stage call since)
+  bool watch_valid = false;
   double w3 = 1.0;
   unsigned int n_inside = 0;
 
@@ -356,6 +358,8 @@ struct Engine : EngineBase {
     r |= alloc(d.srel, ns1); r |= alloc(d.facc, 4 * ns1); r |= alloc(d.fmot, 4 * ns1); r |= alloc(d.dpot, nd1);
     int64_t nbins = (int64_t)kp.nbx * kp.nby * kp.nbz;
     r |= alloc(d.bin_cnt, nbins); r |= alloc(d.bin_list, nbins * BIN_SLOTS);
+    r |= alloc(d.gapf, nbins); r |= alloc(d.watch, n);
+    r |= alloc(d.sph_cnt, ns1); r |= alloc(d.sph_base, ns1);
     if (sizeof(T) == 4) { float4* a = nullptr; r |= alloc(a, kp.ncell_shift); d.acc = a; }
     else { double* a = nullptr; r |= alloc(a, 4 * kp.ncell_shift); d.acc = a; }
     r |= alloc(d.rot, 6 * kp.ncell_shift);
@@ -408,6 +412,7 @@ struct Engine : EngineBase {
     time_count = tc;
     last_rebuild = c - tc;
     last_full = last_rebuild;
+    watch_valid = false;
     return MPCMD_OK;
   }
 
@@ -427,6 +432,7 @@ struct Engine : EngineBase {
   }
 
   int flush_shell() {
+    watch_valid = false;
     if (!home_shell) return MPCMD_OK;
     Launch<T>::flush(d, kp, st);
     home_shell = false;
@@ -520,8 +526,10 @@ struct Engine : EngineBase {
     // free-flight shell members and deferred far particles only between collision steps
     a.horizon = (free_flight && !collision_step) ? steps_to_collision(n) : 0;
     a.full = (!free_flight || collision_step) ? 1 : 0;
-    pb(PROF_BINS); Launch<T>::build_bins(d, kp, a.full ? 0 : a.tc_full, st); pe();
     bool sort_now = cfg.sort_every > 0 && n % cfg.sort_every == 0;
+    if (a.full || sort_now) watch_valid = false;
+    a.use_watch = watch_valid ? 1 : 0;
+    pb(PROF_BINS); Launch<T>::build_bins(d, kp, a.full ? 0 : a.tc_full, st); pe();
     if (sort_now) {
       StepArgs m = a;
       m.merge_only = 1;
@@ -535,12 +543,16 @@ struct Engine : EngineBase {
     }
     pb(PROF_REBUILD); Launch<T>::rebuild(d, kp, a, st); pe();
     pb(PROF_FINALIZE); Launch<T>::finalize_rebuild(d, kp, a, cfg.skin, st); pe();
+    // a collision step's shell is used once before it is sorted into free-flight
+    // and active members; other rebuilds order theirs for the coming steps
+    const bool sorted = (!collision_step || !free_flight) && kp.ns > 0;
+    if (sorted) { pb(PROF_FINALIZE); Launch<T>::sort_shell(d, kp, st); pe(); }
     Counters h;
     int r = read_counters(h);
     if (r) return r;
     if (h.abort_step) return -1;
     if (h.status) return dev_status_to_api(h.status);
-    std::swap(d.sh, d.sh2);
+    if (!sorted) std::swap(d.sh, d.sh2);   // (sort_shell filled d.sh)
     n_inside = h.n_inside;
     time_penetrate = h.time_penetrate;
     time_count = 0;
@@ -554,6 +566,7 @@ struct Engine : EngineBase {
   int prepare() override {
     // main_pattern.f95:168-187 (the reactive grid table is built at create)
     home_shell = false;
+    watch_valid = false;
     advanced = false;
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
     if (kp.ns > 0) Launch<T>::update_srel(d, kp, st);
@@ -565,11 +578,12 @@ struct Engine : EngineBase {
     a.full = 1;
     Launch<T>::rebuild(d, kp, a, st);
     Launch<T>::finalize_rebuild(d, kp, a, cfg.skin, st);
+    Launch<T>::sort_shell(d, kp, st);
     Counters h;
     int r = read_counters(h);
     if (r) return r;
     if (h.status) return dev_status_to_api(h.status);
-    std::swap(d.sh, d.sh2);
+    if (kp.ns == 0) std::swap(d.sh, d.sh2);   // (with spheres sort_shell filled d.sh)
     n_inside = h.n_inside;
     time_penetrate = h.time_penetrate;
     time_count = 0;
@@ -607,7 +621,10 @@ struct Engine : EngineBase {
         // right after a rebuild the shell can be sorted into free-flight and active members
         a.horizon = time_count == 0 ? steps_to_collision(n - 1) : 0;
         pb(PROF_SHELL_ADVANCE); Launch<T>::advance(d, kp, a, st); pe();
-        if (a.horizon > 0) std::swap(d.sh, d.sh2);
+        if (a.horizon > 0) {   // the packed shell in d.sh2 is sorted back into d.sh
+          Launch<T>::sort_shell(d, kp, st);
+          if (kp.ns == 0) std::swap(d.sh, d.sh2);
+        }
         pb(PROF_DIMER); Launch<T>::dimer(d, kp, a, 2, w3, cfg.rattle_max_iter, st); pe();
         advanced = true;
       }
@@ -639,11 +656,21 @@ struct Engine : EngineBase {
       pb(PROF_DIMER); Launch<T>::dimer(d, kp, a, 1 | (last ? 0 : 2), w3, cfg.rattle_max_iter, st); pe();
       if (mpc) {
         pb(PROF_CELLS); Launch<T>::cells(d, kp, a, 1 | (kp.kinetics ? 2 : 0), st); pe();
+        // the rotated velocities hold until the next collision: the particles
+        // that can come near a sphere or a wall before it form the watch list
+        CK(cudaMemsetAsync(&d.ctr->n_watch, 0, sizeof(unsigned int), st));
+        CK(cudaMemsetAsync(&d.ctr->vfar, 0, sizeof(unsigned long long), st));
+        pb(PROF_BINS); Launch<T>::gap_field(d, kp, cfg.mpc_every, st); pe();
+        a.watch_build = cfg.mpc_every;
         pb(PROF_ROTATE_MAIN); Launch<T>::rotate_main(d, kp, a, st); pe();
         StepArgs ar = a;
         ar.horizon = a.advance ? cfg.mpc_every : 0;   // the rebuild of this step was the last one
         pb(PROF_SHELL_ADVANCE); Launch<T>::rotate_shell(d, kp, ar, st); pe();
-        if (ar.horizon > 0) std::swap(d.sh, d.sh2);
+        if (ar.horizon > 0) {
+          pb(PROF_SHELL_ADVANCE); Launch<T>::sort_shell(d, kp, st); pe();
+          if (kp.ns == 0) std::swap(d.sh, d.sh2);
+        }
+        watch_valid = true;
       }
       advanced = !last;
       cstep = n;

@@ -37,6 +37,9 @@ struct Counters {
   unsigned long long vsph;        // bits of the largest sphere speed seen (double)
   unsigned long long vlast;       // bits of max v^2 over all particles at the last rebuild
   unsigned long long vpost;       // bits of max v^2 of the outside particles after the last collision
+  unsigned long long vfar;        // bits of max v^2 of the particles off the watch list
+  unsigned int n_watch;           // entries of the watch list
+  unsigned int watch_pad;
 };
 
 // Bounds check of the checked build (MPCMD_CHECKED): records the first failing
@@ -94,6 +97,10 @@ struct Dev {
   uint8_t* affected;       // [ncell]
   uint8_t* react_box;      // [lx*ly]
   uint32_t* order_rank;    // [ncell] position of each cell in the sort order
+  uint32_t* watch;         // [n] particles that can come near a sphere or a wall before the next collision
+  uint32_t* gapf;          // [nbins] bits of a lower bound on (distance to a sphere - list radius), >= 0
+  uint32_t* sph_cnt;       // [ns] shell entries per first sphere (shell ordering)
+  uint32_t* sph_base;      // [ns] first slot of each sphere's entries
   uint32_t* scnt;          // [ncell] sort scratch
   uint32_t* sstart;        // [ncell]
   uint32_t* sfill;         // [ncell]
@@ -118,6 +125,8 @@ struct StepArgs {
   int g_rebuild;       // SMs x resident blocks of k_rebuild, k_force, k_rotate_main
   int g_force;
   int g_rotate;
+  int watch_build;     // > 0 (the period in steps): rotate_main / rotate_shell build the watch list
+  int use_watch;       // a rebuild between full passes visits the watch list only
   int horizon;         // > 0: steps to the next collision rebuild; shell members that
                        // cannot reach an LJ cutoff or a wall before it fly freely
   double shift[3];     // collision grid shift of this step
@@ -148,6 +157,11 @@ struct Launch {
   static void accumulate_main(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int what, cudaStream_t st);
   static void cells(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int what, cudaStream_t st);
   static void rotate_main(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  // lower bounds of the distance of each bin to the spheres' list radius (for the watch list)
+  static void gap_field(const Dev<T>& d, const KParams<T>& kp, int horizon, cudaStream_t st);
+  // order the shell entries of d.sh2 by their first sphere into d.sh (so that
+  // a warp's particles share spheres); skipped when a displacement abort is pending
+  static void sort_shell(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void rotate_shell(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
   static void flush(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void regather(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);

@@ -51,6 +51,15 @@ __device__ __forceinline__ uint32_t dist_key(int group, uint32_t idx) {
   return ((uint32_t)group << 31) | idx;
 }
 
+// Append i to a list with one atomic per converged group of lanes.
+__device__ __forceinline__ void watch_append(unsigned int* counter, uint32_t* list, uint32_t i) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, g.size());
+  base = g.shfl(base, 0);
+  list[base + g.thread_rank()] = i;
+}
+
 template <typename T>
 __device__ __forceinline__ void block_max_to(unsigned long long* target, double v) {
   __shared__ double red[TPB / 32];
@@ -420,17 +429,24 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   unsigned int pend_old = 0, pend_shift = 0, pend_cnt = 0;
   // The main-array state of the next iteration is loaded before the current
   // one is processed, so that two iterations' loads are in flight.
+  // A rebuild between full passes with a valid watch list visits only the
+  // particles on it: no other particle can enter a list or hit a wall before
+  // the next collision, and their largest speed is kept in vfar.
+  const int64_t nloop = a.use_watch ? (int64_t)d.ctr->n_watch : kp.n;
+  auto pidx = [&](int64_t k) -> int64_t { return a.use_watch ? (int64_t)d.watch[k] : k; };
   const int64_t first = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31) + lane;
   uint8_t pf_f = 0;
   uint32_t pf_cell = 0;
   T pf_ox = 0, pf_oy = 0, pf_oz = 0, pf_vx = 0, pf_vy = 0, pf_vz = 0;
-  if (first < kp.n) {
-    pf_f = d.p.flag[first]; pf_cell = d.p.cell[first];
-    pf_ox = d.p.ox[first]; pf_oy = d.p.oy[first]; pf_oz = d.p.oz[first];
-    pf_vx = d.p.vx[first]; pf_vy = d.p.vy[first]; pf_vz = d.p.vz[first];
+  if (first < nloop) {
+    const int64_t q = pidx(first);
+    pf_f = d.p.flag[q]; pf_cell = d.p.cell[q];
+    pf_ox = d.p.ox[q]; pf_oy = d.p.oy[q]; pf_oz = d.p.oz[q];
+    pf_vx = d.p.vx[q]; pf_vy = d.p.vy[q]; pf_vz = d.p.vz[q];
   }
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < kp.n; base += stride) {
-    const int64_t i = base + lane;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < nloop; base += stride) {
+    const int64_t k = base + lane;
+    const int64_t i = k < nloop ? pidx(k) : kp.n;
     bool dist = false;
     uint32_t cid = 0;
     uint8_t sp = 0;
@@ -438,13 +454,14 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
     uint32_t cell = pf_cell;
     T ox = pf_ox, oy = pf_oy, oz = pf_oz;
     T vx = pf_vx, vy = pf_vy, vz = pf_vz;
-    const int64_t inext = i + stride;
-    if (inext < kp.n) {
-      pf_f = d.p.flag[inext]; pf_cell = d.p.cell[inext];
-      pf_ox = d.p.ox[inext]; pf_oy = d.p.oy[inext]; pf_oz = d.p.oz[inext];
-      pf_vx = d.p.vx[inext]; pf_vy = d.p.vy[inext]; pf_vz = d.p.vz[inext];
+    const int64_t knext = k + stride;
+    if (knext < nloop) {
+      const int64_t q = pidx(knext);
+      pf_f = d.p.flag[q]; pf_cell = d.p.cell[q];
+      pf_ox = d.p.ox[q]; pf_oy = d.p.oy[q]; pf_oz = d.p.oz[q];
+      pf_vx = d.p.vx[q]; pf_vy = d.p.vy[q]; pf_vz = d.p.vz[q];
     }
-    if (i < kp.n) {
+    if (k < nloop) {
       const uint32_t cell0 = cell;
       const T vx0 = vx, vy0 = vy, vz0 = vz;
       const bool from_shell = (f & FLAG_HOME_SHELL) != 0;
@@ -607,6 +624,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   }
   if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
     atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
+  if (a.use_watch && blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&d.ctr->maxv2, d.ctr->vfar);
   block_max_to<T>(&d.ctr->maxv2, (double)vmax2);
 }
 
@@ -870,6 +888,7 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
           min_gap = gap < min_gap ? gap : min_gap;
         }
         const uint32_t idx = d.sh.idx[j];
+        if (a.watch_build) watch_append(&d.ctr->n_watch, d.watch, idx);
         const T msd_now = d.sh.msd[j];
         if (free_flight_ok(kp, cell, oz, vx, vy, vz, msd_now, min_gap, a.horizon, vs)) {
           // state of this step into the main home; no force acts before the
@@ -909,6 +928,7 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
       d.sh.ox[j] = ox; d.sh.oy[j] = oy; d.sh.oz[j] = oz;
       d.sh.flag[j] = fl;
     }
+    if (a.watch_build) watch_append(&d.ctr->n_watch, d.watch, d.sh.idx[j]);
     d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
   }
   if (a.advance) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], (double)msdmax);
@@ -941,6 +961,104 @@ void Launch<T>::rotate_shell(const Dev<T>& d, const KParams<T>& kp, const StepAr
     k_shell_commit<T><<<1, 1, 0, st>>>(d.ctr, d.sh2.cap);
     LAUNCH_COUNT();
   }
+}
+
+// ------------------------------------------------------- shell ordering ----
+// Counting sort of the shell entries by their first sphere: the entries a warp
+// processes then mostly share their spheres, so the per-sphere warp
+// reductions of k_force run once or twice per warp instead of once per sphere
+// present.  The order within a sphere is not specified (results do not depend
+// on it beyond the summation order of the FP64 sphere-force atomics).
+template <typename T>
+__global__ void k_shell_hist(Dev<T> d, KParams<T> kp) {
+  if (d.ctr->abort_step) return;
+  const unsigned int nin = d.ctr->n_inside;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < (int64_t)nin; base += stride) {
+    const int64_t j = base + lane;
+    int s = -1;
+    if (j < (int64_t)nin) {
+      s = d.sh2.sph[(size_t)j * PAIRMAX];
+      if (!chk(s < kp.ns, d.ctr, 123, s)) s = -1;
+    }
+    // one atomic per sphere present in the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, s);
+    if (s >= 0 && lane == __ffs(peers) - 1) atomicAdd(&d.sph_cnt[s], (unsigned)__popc(peers));
+  }
+}
+
+template <typename T>
+__global__ void k_shell_scan(Dev<T> d, KParams<T> kp) {
+  if (d.ctr->abort_step) return;
+  // one block: exclusive scan of the ns counts, which become the cursors
+  __shared__ uint32_t part[TPB];
+  const int per = (kp.ns + TPB - 1) / TPB;
+  const int lo = threadIdx.x * per, hi = min(lo + per, kp.ns);
+  uint32_t sum = 0;
+  for (int s = lo; s < hi; ++s) sum += d.sph_cnt[s];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int t = 0; t < TPB; ++t) { const uint32_t v = part[t]; part[t] = run; run += v; }
+  }
+  __syncthreads();
+  uint32_t run = part[threadIdx.x];
+  for (int s = lo; s < hi; ++s) { const uint32_t v = d.sph_cnt[s]; d.sph_base[s] = run; d.sph_cnt[s] = 0; run += v; }
+}
+
+template <typename T>
+__global__ void k_shell_scatter(Dev<T> d, KParams<T> kp) {
+  if (d.ctr->abort_step) return;
+  const unsigned int nin = d.ctr->n_inside;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < (int64_t)nin; base += stride) {
+    const int64_t j = base + lane;
+    uint4 packed = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    int s = -1;
+    if (j < (int64_t)nin) {
+      packed = *reinterpret_cast<const uint4*>(d.sh2.sph + (size_t)j * PAIRMAX);
+      s = (int)(packed.x & 0xFFFFu);
+      if (!chk(s < kp.ns, d.ctr, 124, s)) s = -1;
+    }
+    // one atomic per sphere present in the warp; its lanes take consecutive slots
+    const unsigned peers = __match_any_sync(0xffffffffu, s);
+    const int lead = __ffs(peers) - 1;
+    uint32_t first = 0;
+    if (s >= 0 && lane == lead) first = atomicAdd(&d.sph_cnt[s], (unsigned)__popc(peers));
+    first = __shfl_sync(0xffffffffu, first, lead);
+    if (s < 0) continue;
+    const uint32_t k = d.sph_base[s] + first + __popc(peers & ((1u << lane) - 1u));
+    if (!chk((int64_t)k < d.sh.cap, d.ctr, 125, k)) continue;
+    const uint32_t idx = d.sh2.idx[j];
+    d.sh.idx[k] = idx;
+    d.sh.cell[k] = d.sh2.cell[j];
+    d.sh.ox[k] = d.sh2.ox[j]; d.sh.oy[k] = d.sh2.oy[j]; d.sh.oz[k] = d.sh2.oz[j];
+    d.sh.vx[k] = d.sh2.vx[j]; d.sh.vy[k] = d.sh2.vy[j]; d.sh.vz[k] = d.sh2.vz[j];
+    d.sh.msd[k] = d.sh2.msd[j];
+    d.sh.flag[k] = d.sh2.flag[j];
+    d.sh.nonbulk[k] = d.sh2.nonbulk[j];
+    d.sh.np[k] = d.sh2.np[j];
+    *reinterpret_cast<uint4*>(d.sh.sph + (size_t)k * PAIRMAX) = packed;
+    d.p.cell[idx] = k;
+  }
+}
+
+template <typename T>
+__global__ void k_shell_clear_counts(Dev<T> d, KParams<T> kp) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < kp.ns; s += gridDim.x * blockDim.x) d.sph_cnt[s] = 0u;
+}
+
+template <typename T>
+void Launch<T>::sort_shell(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
+  if (kp.ns == 0) return;
+  k_shell_clear_counts<T><<<(kp.ns + TPB - 1) / TPB, TPB, 0, st>>>(d, kp);
+  k_shell_hist<T><<<1024, TPB, 0, st>>>(d, kp);
+  k_shell_scan<T><<<1, TPB, 0, st>>>(d, kp);
+  k_shell_scatter<T><<<1024, TPB, 0, st>>>(d, kp);
+  LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT();
 }
 
 // ---------------------------------------------------------------- dimers ----
@@ -1385,6 +1503,78 @@ void Launch<T>::cells(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, 
   LAUNCH_COUNT();
 }
 
+// Watch list support: for every coarse bin, a lower bound on the distance
+// from any point of the bin to the list radius (r_c 2^(1/6) + skin) of any
+// sphere, clamped at 0 (float bits, so atomicMin orders them).  Bins farther
+// than the largest flight of the coming period keep the initial huge value.
+template <typename T>
+__global__ void k_gap_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn, int horizon) {
+  const int s = blockIdx.x;
+  if (s >= kp.ns) return;
+  const double Rl = (s & 1) ? Rn : Rc;
+  // |v'| <= |v| + 2 |v_cm| <= 3 vmax after the collision (vmax of the last
+  // rebuild); the spheres move at most vs; one cell of margin
+  const double vmax = sqrt(__longlong_as_double((long long)d.ctr->vlast));
+  const double vs = (double)sphere_speed_bound<T>(d.ctr);
+  const double reach = (3.0 * vmax + vs) * kp.dtd * (double)horizon + 1.0;
+  const double hd = 0.5 * sqrt(3.0) * (double)BIN_EDGE;
+  const double Rm = Rl + reach + hd;
+  const int nb[3] = {kp.nbx, kp.nby, kp.nbz};
+  const double L[3] = {(double)kp.lx, (double)kp.ly, (double)kp.lz};
+  const bool per[3] = {true, true, kp.geometry == 1};
+  double X[3];
+  int lo[3], hi[3];
+  for (int q = 0; q < 3; ++q) {
+    X[q] = d.dpos[3 * s + q];
+    lo[q] = (int)floor((X[q] - Rm) / (double)BIN_EDGE);
+    hi[q] = (int)floor((X[q] + Rm) / (double)BIN_EDGE);
+    if (!per[q]) { lo[q] = max(lo[q], 0); hi[q] = min(hi[q], nb[q] - 1); }
+    else if (hi[q] - lo[q] + 1 >= nb[q]) { lo[q] = 0; hi[q] = nb[q] - 1; }
+  }
+  const int n0 = hi[0] - lo[0] + 1, n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1;
+  const int tot = n0 * n1 * n2;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    int w[3] = {lo[0] + t % n0, lo[1] + (t / n0) % n1, lo[2] + t / (n0 * n1)};
+    double d2 = 0.0;
+    for (int q = 0; q < 3; ++q) {
+      if (per[q]) w[q] = ((w[q] % nb[q]) + nb[q]) % nb[q];
+      double dc = (double)w[q] * BIN_EDGE + 0.5 * BIN_EDGE - X[q];
+      if (per[q]) dc = dmin_image(dc, L[q]);
+      d2 += dc * dc;
+    }
+    double lb = sqrt(d2) - hd - Rl;
+    if (lb < 0.0) lb = 0.0;
+    const int b = w[0] + nb[0] * (w[1] + nb[1] * w[2]);
+    if (!chk(b >= 0 && b < nb[0] * nb[1] * nb[2], d.ctr, 122, b)) continue;
+    atomicMin(&d.gapf[b], __float_as_uint((float)lb));
+  }
+}
+
+template <typename T>
+void Launch<T>::gap_field(const Dev<T>& d, const KParams<T>& kp, int horizon, cudaStream_t st) {
+  const int nbins = kp.nbx * kp.nby * kp.nbz;
+  cudaMemsetAsync(d.gapf, 0x7F, sizeof(uint32_t) * nbins, st);   // 3.4e38
+  if (kp.ns == 0) return;
+  const double Rc = sqrt((double)kp.full2[0]) + 1e-6, Rn = sqrt((double)kp.full2[1]) + 1e-6;
+  k_gap_fill<T><<<kp.ns, 256, 0, st>>>(d, kp, Rc, Rn, horizon);
+  LAUNCH_COUNT();
+}
+
+// Watch-list test of an outside particle after the collision: can it come
+// within the list radius of a sphere (gap: the gap field of its bin), or hit
+// a wall, before the next collision (`horizon` steps at speed sqrt(v2))?
+template <typename T>
+__device__ __forceinline__ bool watch_test(const KParams<T>& kp, T gap, uint32_t cell, T vz, T v2, int horizon,
+                                           T vs) {
+  const T t = kp.dt * (T)horizon;
+  if (gap < (T)1e30 && gap <= (sqrt(v2) + vs) * t + (T)0.1) return true;
+  if (kp.geometry == 0) {
+    const T cz = (T)cell_z(cell), dz = fabs(vz) * t;
+    if (cz - dz < (T)0.05 || cz + (T)1 + dz > (T)kp.lz - (T)0.05) return true;
+  }
+  return false;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
@@ -1392,6 +1582,11 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
   // are issued before the first store
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   T vmax2 = (T)0;   // speed bound of the outside particles until the next collision
+  // with a.watch_build (= the period in steps): the particles that can come
+  // near a sphere or a wall before the next collision join the watch list;
+  // vfar2 is the largest v^2 of the others (constant until that collision)
+  T vfar2 = (T)0;
+  const T vs = sphere_speed_bound<T>(d.ctr);
   for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < kp.n; i0 += 2 * stride) {
     const int64_t i1 = i0 + stride;
     const bool h1 = i1 < kp.n;
@@ -1403,26 +1598,49 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
     T vx1 = (T)0, vy1 = (T)0, vz1 = (T)0;
     if (h1) { vx1 = d.p.vx[i1]; vy1 = d.p.vy[i1]; vz1 = d.p.vz[i1]; }
     const bool r0 = !(f0 & FLAG_HOME_SHELL), r1 = !(f1 & FLAG_HOME_SHELL);
+    // watch-list inputs, loaded with the rest before any store
+    uint32_t c0 = 0, c1 = 0;
+    if (a.watch_build) {
+      if (r0) c0 = d.p.cell[i0];
+      if (r1) c1 = d.p.cell[i1];
+    }
     T t0[6], t1[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
       t0[q] = r0 ? d.rot[6 * (size_t)k0 + q] : (T)0;
       t1[q] = r1 ? d.rot[6 * (size_t)k1 + q] : (T)0;
     }
+    T g0 = (T)3e38, g1 = (T)3e38;
+    if (a.watch_build) {
+      if (r0) g0 = __uint_as_float(d.gapf[bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, c0)]);
+      if (r1) g1 = __uint_as_float(d.gapf[bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, c1)]);
+    }
     if (r0) {
       rotate_v(kp, t0, vx0, vy0, vz0);
       d.p.vx[i0] = vx0; d.p.vy[i0] = vy0; d.p.vz[i0] = vz0;
       const T w = vx0 * vx0 + vy0 * vy0 + vz0 * vz0;
       vmax2 = w > vmax2 ? w : vmax2;
+      if (a.watch_build) {
+        if (watch_test(kp, g0, c0, vz0, w, a.watch_build, vs)) watch_append(&d.ctr->n_watch, d.watch, (uint32_t)i0);
+        else vfar2 = w > vfar2 ? w : vfar2;
+      }
     }
     if (r1) {
       rotate_v(kp, t1, vx1, vy1, vz1);
       d.p.vx[i1] = vx1; d.p.vy[i1] = vy1; d.p.vz[i1] = vz1;
       const T w = vx1 * vx1 + vy1 * vy1 + vz1 * vz1;
       vmax2 = w > vmax2 ? w : vmax2;
+      if (a.watch_build) {
+        if (watch_test(kp, g1, c1, vz1, w, a.watch_build, vs)) watch_append(&d.ctr->n_watch, d.watch, (uint32_t)i1);
+        else vfar2 = w > vfar2 ? w : vfar2;
+      }
     }
   }
   block_max_to<T>(&d.ctr->vpost, (double)vmax2);
+  if (a.watch_build) {
+    __syncthreads();   // block_max_to's shared buffer is reused
+    block_max_to<T>(&d.ctr->vfar, (double)vfar2);
+  }
 }
 
 template <typename T>
