@@ -1194,7 +1194,18 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
       double Con1diff = (dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) - Dcn * Dcn;
       if (fabs(Con1diff) < 1.e-6) break;
       if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
-      double G = -(0.25 * Con1diff * IIM / (dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2]));
+      const double den = dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2];
+      double G;
+      if (fast) {
+        // the iteration converges to the tolerance whatever the last bits of
+        // G are: a float reciprocal refined twice replaces the division
+        double r = (double)__frcp_rn((float)den);
+        r = r * (2.0 - den * r);
+        r = r * (2.0 - den * r);
+        G = -(0.25 * Con1diff * IIM) * r;
+      } else {
+        G = -(0.25 * Con1diff * IIM / den);
+      }
       if (fast) {
         const double G2 = 2.0 * G;
         for (int c = 0; c < 3; ++c) {
@@ -1220,9 +1231,13 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
       acc++;
     }
     if (fast) {
+      // one step moves a sphere far less than a box edge: a single shift
       for (int c = 0; c < nwrap; ++c) {
-        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
-        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+        const double L = kp.Ld[c];
+        if (X1[c] >= L) X1[c] -= L; else if (X1[c] < 0.0) X1[c] += L;
+        if (X2[c] >= L) X2[c] -= L; else if (X2[c] < 0.0) X2[c] += L;
+        if (!(X1[c] >= 0.0 && X1[c] < L)) X1[c] = X1[c] - L * floor(X1[c] / L);
+        if (!(X2[c] >= 0.0 && X2[c] < L)) X2[c] = X2[c] - L * floor(X2[c] / L);
       }
     }
     iters += acc;
