@@ -42,7 +42,7 @@ FALLBACK_HBM = 6800.0
 BYTES_PER_PARTICLE_REBUILD = 46      # read flag+cell+offset+velocity (29 B), write cell+offset+flag (17 B)
 BYTES_PER_SHELL_ENTRY = 84           # shell entry written (55 B) and the previous shell entry read (29 B)
 BYTES_PER_SHELL_FORCE = 87           # shell particle read (54 B) and written back (33 B) per MD step
-BYTES_PER_PARTICLE_ROTATE = 29       # flag + shifted key + velocity read, velocity written
+BYTES_PER_PARTICLE_ROTATE = 33       # flag + shifted key + cell + velocity read, velocity written
 BYTES_PER_CELL = 56                  # collision accumulator read + reset (32 B), rotation table written (24 B)
 BYTES_PER_CELL_REACTION = 74         # packed counts + first keys + affected, read and reset
 
@@ -214,22 +214,28 @@ def gpu_arm(args, ws, rk, lr, dist):
     e.run(args.steps * S)
     prof = e.profile_read()
     e.profile(False)
-    ob = e.observables()
-    n_in = ob["n_inside"]
+    work = e.counters()   # device work totals of pass B
     ncs = e.n_cells_shifted()
     nc = e.ncell
 
+    def per_launch(total, kind):
+        return total / max(prof[kind][1], 1)
+
     def bytes_per_launch(kind):
+        # the work each kernel did, averaged over its launches: the rebuilds
+        # between collisions visit only the watch list, the force kernel only
+        # the active shell entries
         if kind == "rebuild":
-            return N * BYTES_PER_PARTICLE_REBUILD + n_in * BYTES_PER_SHELL_ENTRY, N, "particles"
+            vis = per_launch(work["work_rebuild_particles"], "rebuild")
+            placed = per_launch(work["work_rebuild_placed"], "rebuild")
+            return vis * BYTES_PER_PARTICLE_REBUILD + placed * BYTES_PER_SHELL_ENTRY, vis, "particles visited"
         if kind == "force":
-            return n_in * BYTES_PER_SHELL_FORCE, n_in, "shell particles"
+            ent = per_launch(work["work_force_entries"], "force")
+            return ent * BYTES_PER_SHELL_FORCE, ent, "active shell entries"
         if kind == "rotate_main":
             return N * BYTES_PER_PARTICLE_ROTATE, N, "particles"
         if kind == "cells":
             return ncs * BYTES_PER_CELL + nc * BYTES_PER_CELL_REACTION, ncs, "cells"
-        if kind == "shell_advance":
-            return n_in * BYTES_PER_SHELL_FORCE, n_in, "shell particles"
         return None, None, None
 
     kinds = sorted(prof, key=lambda k: -prof[k][0])

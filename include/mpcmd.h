@@ -143,6 +143,11 @@ int mpcmd_get_shift(mpcmd_ctx* ctx, double* shift);
 int mpcmd_get_pairs(mpcmd_ctx* ctx, int64_t* n_pairs, int64_t* particle, int32_t* sphere);
 /* The inside list (neighbour_list_mod.f95 inout_particle_list) of the last rebuild. */
 int mpcmd_get_inside(mpcmd_ctx* ctx, int64_t* n_inside, int64_t* idx);
+/* Up to n of: shell entries, device status bits, time_penetrate, RATTLE
+ * iterations, cstep, time_count, pending abort step, last rebuild step,
+ * checked-build failure code and value, watch-list entries, and since the last
+ * mpcmd_profile(ctx, 1): shell entries over all force launches, particles
+ * visited over all rebuild launches, shell entries written by the rebuilds. */
 int mpcmd_get_counters(mpcmd_ctx* ctx, int64_t* counters, int32_t n);
 int mpcmd_reactive_grid_table(mpcmd_ctx* ctx, int32_t* table);
 int mpcmd_cell_order(mpcmd_ctx* ctx, int32_t* order);

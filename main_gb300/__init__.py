@@ -293,10 +293,11 @@ class Engine:
         return part[sph == sphere]
 
     def counters(self):
-        c = np.zeros(10, dtype=np.int64)
-        self._c(lib().mpcmd_get_counters(self.h, _ptr(c, C.c_int64), 10), "get_counters")
+        c = np.zeros(14, dtype=np.int64)
+        self._c(lib().mpcmd_get_counters(self.h, _ptr(c, C.c_int64), 14), "get_counters")
         keys = ("n_inside", "status", "time_penetrate", "rattle_iters", "cstep", "time_count", "abort_step",
-                "last_rebuild", "dbg_code", "dbg_val")
+                "last_rebuild", "dbg_code", "dbg_val", "n_watch", "work_force_entries", "work_rebuild_particles",
+                "work_rebuild_placed")
         return dict(zip(keys, (int(v) for v in c)))
 
     def reactive_grid(self):

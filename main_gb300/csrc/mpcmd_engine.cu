@@ -959,10 +959,11 @@ struct Engine : EngineBase {
     Counters h;
     int r = read_counters(h);
     if (r) return r;
-    int64_t v[10] = {(int64_t)h.n_inside, (int64_t)h.status, (int64_t)h.time_penetrate, (int64_t)h.rattle_iters,
+    int64_t v[14] = {(int64_t)h.n_inside, (int64_t)h.status, (int64_t)h.time_penetrate, (int64_t)h.rattle_iters,
                      (int64_t)cstep, (int64_t)time_count, (int64_t)h.abort_step, (int64_t)last_rebuild,
-                     (int64_t)h.dbg_code, (int64_t)h.dbg_val};
-    for (int q = 0; q < n && q < 10; ++q) c[q] = v[q];
+                     (int64_t)h.dbg_code, (int64_t)h.dbg_val, (int64_t)h.n_watch, (int64_t)h.acc_force,
+                     (int64_t)h.acc_rebuild, (int64_t)h.acc_placed};
+    for (int q = 0; q < n && q < 14; ++q) c[q] = v[q];
     return MPCMD_OK;
   }
 
@@ -990,7 +991,10 @@ struct Engine : EngineBase {
   int profile(int enable) override {
     prof_collect();
     profiling = enable != 0;
-    if (enable) for (int k = 0; k < PROF_KINDS; ++k) { prof_ms[k] = 0.; prof_n[k] = 0; }
+    if (enable) {
+      for (int k = 0; k < PROF_KINDS; ++k) { prof_ms[k] = 0.; prof_n[k] = 0; }
+      CK(cudaMemsetAsync(&d.ctr->acc_force, 0, 3 * sizeof(unsigned long long), st));
+    }
     return MPCMD_OK;
   }
   int profile_read(double* ms, int64_t* count, int n) override {

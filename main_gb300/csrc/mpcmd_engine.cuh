@@ -40,6 +40,10 @@ struct Counters {
   unsigned long long vfar;        // bits of max v^2 of the particles off the watch list
   unsigned int n_watch;           // entries of the watch list
   unsigned int watch_pad;
+  // work totals for the measurement (cleared by mpcmd_profile(ctx, 1))
+  unsigned long long acc_force;   // shell entries over all k_force launches
+  unsigned long long acc_rebuild; // particles visited over all k_rebuild launches
+  unsigned long long acc_placed;  // shell entries written by the rebuilds
 };
 
 // Bounds check of the checked build (MPCMD_CHECKED): records the first failing

@@ -433,6 +433,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   // particles on it: no other particle can enter a list or hit a wall before
   // the next collision, and their largest speed is kept in vfar.
   const int64_t nloop = a.use_watch ? (int64_t)d.ctr->n_watch : kp.n;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_rebuild, (unsigned long long)nloop);
   auto pidx = [&](int64_t k) -> int64_t { return a.use_watch ? (int64_t)d.watch[k] : k; };
   const int64_t first = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31) + lane;
   uint8_t pf_f = 0;
@@ -647,6 +648,7 @@ __global__ void k_finalize(Dev<T> d, KParams<T> kp, StepArgs a, double skin) {
   if (!a.merge_only) {
     unsigned int m = d.ctr->n_inside_new;
     if ((int64_t)m > d.sh2.cap) m = (unsigned int)d.sh2.cap;   // overflow is reported via status
+    d.ctr->acc_placed += m;
     d.ctr->n_inside = m;
     d.ctr->n_inside_new = 0u;
   }
@@ -726,6 +728,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
     return;
   }
   const unsigned int nin = d.ctr->n_inside;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_force, (unsigned long long)nin);
   const int64_t stride = (int64_t)a.g_force * blockDim.x;
   const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
   const int lane = threadIdx.x & 31;
