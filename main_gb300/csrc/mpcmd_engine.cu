@@ -494,6 +494,7 @@ struct Engine : EngineBase {
     a.grid = grid;
     a.g_rebuild = g_rebuild; a.g_force = g_force; a.g_rotate = g_rotate;
     a.shift[0] = shift[0]; a.shift[1] = shift[1]; a.shift[2] = shift[2];
+    for (int c = 0; c < 3; ++c) a.shf[c] = (float)shift[c];
     return a;
   }
 

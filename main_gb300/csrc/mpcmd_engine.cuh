@@ -134,6 +134,7 @@ struct StepArgs {
   int horizon;         // > 0: steps to the next collision rebuild; shell members that
                        // cannot reach an LJ cutoff or a wall before it fly freely
   double shift[3];     // collision grid shift of this step
+  float shf[3];        // the same rounded to float (FP32 kernels)
 };
 
 template <typename T>

@@ -60,20 +60,31 @@ __device__ __forceinline__ void watch_append(unsigned int* counter, uint32_t* li
   list[base + g.thread_rank()] = i;
 }
 
+// Block maximum of a non-negative value, folded into the double bits at
+// target.  The reduction runs in T; only the block's result is widened (FP64
+// instructions are slow on this part).
 template <typename T>
-__device__ __forceinline__ void block_max_to(unsigned long long* target, double v) {
-  __shared__ double red[TPB / 32];
-  double m = v;
+__device__ __forceinline__ void block_max_to(unsigned long long* target, T v) {
+  __shared__ T red[TPB / 32];
+  T m = v;
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) red[w] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double b = red[0];
+    T b = red[0];
     for (int i = 1; i < (int)(blockDim.x >> 5); ++i) b = fmax(b, red[i]);
-    if (b > 0) atomicMax(target, ord_bits(b));
+    if (b > (T)0) atomicMax(target, ord_bits(to_f64(b)));
   }
 }
+
+// Grid shift of the step in T (the host rounds it to float once).
+template <typename T>
+__device__ __forceinline__ T step_shift(const StepArgs& a, int c);
+template <>
+__device__ __forceinline__ float step_shift<float>(const StepArgs& a, int c) { return a.shf[c]; }
+template <>
+__device__ __forceinline__ double step_shift<double>(const StepArgs& a, int c) { return a.shift[c]; }
 
 // Sum of (fx, fy, fz, u) over the lanes of a converged warp that hold the same
 // sphere s (s < 0: nothing), added once per distinct sphere to facc[4s..4s+3].
@@ -95,10 +106,10 @@ __device__ __forceinline__ void warp_sphere_add(double* facc, int s, T fx, T fy,
       a3 += __shfl_xor_sync(full, a3, o);
     }
     if (lane == src) {
-      atomicAdd(&facc[4 * sr + 0], (double)a0);
-      atomicAdd(&facc[4 * sr + 1], (double)a1);
-      atomicAdd(&facc[4 * sr + 2], (double)a2);
-      atomicAdd(&facc[4 * sr + 3], (double)a3);
+      atomicAdd(&facc[4 * sr + 0], to_f64(a0));
+      atomicAdd(&facc[4 * sr + 1], to_f64(a1));
+      atomicAdd(&facc[4 * sr + 2], to_f64(a2));
+      atomicAdd(&facc[4 * sr + 3], to_f64(a3));
     }
     remaining &= ~grp;
   }
@@ -420,7 +431,7 @@ __device__ __forceinline__ T sphere_speed_bound(const Counters* c) {
 template <typename T>
 __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
-  const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
+  const T sx = step_shift<T>(a, 0), sy = step_shift<T>(a, 1), sz = step_shift<T>(a, 2);
   T vmax2 = (T)0;
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -433,6 +444,9 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   // particles on it: no other particle can enter a list or hit a wall before
   // the next collision, and their largest speed is kept in vfar.
   const int64_t nloop = a.use_watch ? (int64_t)d.ctr->n_watch : kp.n;
+  // sphere speed bound of the free-flight test, read once (FP64 arithmetic
+  // is slow on this part)
+  const T vs_bound = (a.horizon > 0 && !a.mpc) ? sphere_speed_bound<T>(d.ctr) : (T)0;
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_rebuild, (unsigned long long)nloop);
   auto pidx = [&](int64_t k) -> int64_t { return a.use_watch ? (int64_t)d.watch[k] : k; };
   const int64_t first = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31) + lane;
@@ -550,8 +564,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
         // a free-flight member must not have entered a cutoff since it was classified
         if ((f & FLAG_PASSIVE) && nonbulk) atomicOr(&d.ctr->status, DEV_ERR_PASSIVE);
         const bool passive = np > 0 && a.horizon > 0 && !a.mpc &&
-                             free_flight_ok(kp, cell, oz, vx, vy, vz, (T)0, min_gap, a.horizon,
-                                            sphere_speed_bound<T>(d.ctr));
+                             free_flight_ok(kp, cell, oz, vx, vy, vz, (T)0, min_gap, a.horizon, vs_bound);
         const uint8_t nf = passive ? (uint8_t)(sp | FLAG_PASSIVE) : sp;
         bool placed = false;
         if (np > 0 && !passive) {
@@ -609,8 +622,11 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
     // (cell, species) group of the warp; the group's lowest lane holds its
     // smallest particle index
     if (a.mpc && kp.kinetics != 0 && !a.merge_only) {
-      const unsigned long long mk = dist ? (((unsigned long long)cid << 2) | sp) : ~0ull;
-      const unsigned peers = __match_any_sync(0xffffffffu, mk);
+      // 32-bit key (cid < 2^30 since every box edge is at most 1024 cells);
+      // a 64-bit match costs twice the SM cycles of a 32-bit one
+      const unsigned dmask = __ballot_sync(0xffffffffu, dist);
+      unsigned peers = 0u;
+      if (dist) peers = __match_any_sync(dmask, (cid << 2) | (uint32_t)sp);
       if (dist && lane == __ffs(peers) - 1) {
         // the count returned by this atomic is checked one iteration later,
         // so that the warp does not wait for it
@@ -626,7 +642,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
     atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
   if (a.use_watch && blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&d.ctr->maxv2, d.ctr->vfar);
-  block_max_to<T>(&d.ctr->maxv2, (double)vmax2);
+  block_max_to<T>(&d.ctr->maxv2, vmax2);
 }
 
 template <typename T>
@@ -673,8 +689,9 @@ template <typename T>
 __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
   if (!a.rebuilt) {
-    double m = __longlong_as_double((long long)d.ctr->maxmsd[a.step & 1]);
-    if (m > (double)kp.msd_thr) {
+    // max_solvent_dist > threshold, compared on the double bits (both >= 0)
+    const unsigned long long thr = (unsigned long long)__double_as_longlong(to_f64(kp.msd_thr));
+    if (d.ctr->maxmsd[a.step & 1] > thr) {
       if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&d.ctr->abort_step, 0, (int)a.step);
       return;
     }
@@ -730,7 +747,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
   const unsigned int nin = d.ctr->n_inside;
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_force, (unsigned long long)nin);
   const int64_t stride = (int64_t)a.g_force * blockDim.x;
-  const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
+  const T sx = step_shift<T>(a, 0), sy = step_shift<T>(a, 1), sz = step_shift<T>(a, 2);
   const int lane = threadIdx.x & 31;
   T msdmax = (T)0;
   // warp-aligned grid-stride loop: a warp stays converged for the per-sphere
@@ -831,7 +848,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
       d.sh.flag[j] = fl;
     }
   }
-  if (a.advance && !a.mpc) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], (double)msdmax);
+  if (a.advance && !a.mpc) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], msdmax);
 }
 
 template <typename T>
@@ -934,7 +951,7 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
     if (a.watch_build) watch_append(&d.ctr->n_watch, d.watch, d.sh.idx[j]);
     d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
   }
-  if (a.advance) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], (double)msdmax);
+  if (a.advance) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], msdmax);
 }
 
 // Publish the shell packed by k_shell_advance.
@@ -1312,7 +1329,7 @@ void Launch<T>::affected(const Dev<T>& d, const KParams<T>& kp, const StepArgs& 
 // collision, bit 1: distribute.
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_accumulate_main(Dev<T> d, KParams<T> kp, StepArgs a, int what) {
-  const T sx = (T)a.shift[0], sy = (T)a.shift[1], sz = (T)a.shift[2];
+  const T sx = step_shift<T>(a, 0), sy = step_shift<T>(a, 1), sz = step_shift<T>(a, 2);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
     uint32_t cell = d.p.cell[i];
@@ -1654,10 +1671,10 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
       }
     }
   }
-  block_max_to<T>(&d.ctr->vpost, (double)vmax2);
+  block_max_to<T>(&d.ctr->vpost, vmax2);
   if (a.watch_build) {
     __syncthreads();   // block_max_to's shared buffer is reused
-    block_max_to<T>(&d.ctr->vfar, (double)vfar2);
+    block_max_to<T>(&d.ctr->vfar, vfar2);
   }
 }
 
