@@ -320,6 +320,9 @@ __device__ __forceinline__ bool bin_first(int c, int lo, int L, bool wraps, int&
   return true;
 }
 
+// Bins along one axis: box edges are at most 1024 cells, bins BIN_EDGE wide.
+constexpr int MAX_BINS_PER_AXIS = 1024 / BIN_EDGE;
+
 template <typename T>
 __global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn, int tc_defer) {
   const int s = blockIdx.x;
@@ -338,20 +341,29 @@ __global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn, int t
     const double* V = d.dvel + 3 * s;
     atomicMax(&d.ctr->vsph, ord_bits(sqrt(V[0] * V[0] + V[1] * V[1] + V[2] * V[2])));
   }
-  int lo[3], hi[3];
-  bool wr[3];
-  const int L[3] = {kp.lx, kp.ly, kp.lz};
-  const bool per[3] = {true, true, kp.geometry == 1};
-  for (int q = 0; q < 3; ++q) wr[q] = axis_range(d.dpos[3 * s + q], R, L[q], per[q], lo[q], hi[q]);
-  const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+  // per axis, the bins the cell range [lo, hi] enters (each once), listed by
+  // one thread each; then one thread per bin of the product
+  __shared__ int16_t blist[3][MAX_BINS_PER_AXIS];
+  __shared__ int nbl[3];
+  if (threadIdx.x < 3) {
+    const int q = threadIdx.x;
+    const int L = q == 0 ? kp.lx : (q == 1 ? kp.ly : kp.lz);
+    const bool per = q < 2 || kp.geometry == 1;
+    int lo, hi;
+    const bool wr = axis_range(d.dpos[3 * s + q], R, L, per, lo, hi);
+    int m = 0;
+    for (int c = lo; c <= hi; ++c) {
+      int b;
+      if (bin_first(c, lo, L, wr, b) && m < MAX_BINS_PER_AXIS) blist[q][m++] = (int16_t)b;
+    }
+    nbl[q] = m;
+  }
+  __syncthreads();
+  const int nx = nbl[0], ny = nbl[1], nz = nbl[2];
   const int tot = nx * ny * nz;
   const int nbins = kp.nbx * kp.nby * kp.nbz;
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int cx = lo[0] + t % nx, cy = lo[1] + (t / nx) % ny, cz = lo[2] + t / (nx * ny);
-    int bx, by, bz;
-    if (!bin_first(cx, lo[0], L[0], wr[0], bx)) continue;
-    if (!bin_first(cy, lo[1], L[1], wr[1], by)) continue;
-    if (!bin_first(cz, lo[2], L[2], wr[2], bz)) continue;
+    const int bx = blist[0][t % nx], by = blist[1][(t / nx) % ny], bz = blist[2][t / (nx * ny)];
     int bin = bx + kp.nbx * (by + kp.nby * bz);
     if (!chk(bin >= 0 && bin < nbins, d.ctr, 108, bin)) continue;
     unsigned int slot = atomicAdd(&d.bin_cnt[bin], 1u);
