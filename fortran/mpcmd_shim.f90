@@ -62,6 +62,13 @@ module mpcmd_shim
     integer(c_int32_t) :: reserved(6)
   end type mpcmd_config
 
+  ! struct mpcmd_conc_params
+  type, bind(C), public :: mpcmd_conc_params
+    real(c_double) :: x_slab, y_slab, z_slab
+    real(c_double) :: half_width
+    real(c_double) :: x_width, y_width, z_width
+  end type mpcmd_conc_params
+
   ! struct mpcmd_obs
   type, bind(C), public :: mpcmd_obs
     real(c_double) :: momentum(3)
@@ -77,6 +84,7 @@ module mpcmd_shim
   public :: mpcmd_set_step, mpcmd_initial, mpcmd_prepare, mpcmd_step, mpcmd_evolve, mpcmd_run
   public :: mpcmd_sort, mpcmd_rebuild_lists, mpcmd_distribute, mpcmd_mpc_rotation, mpcmd_reaction
   public :: mpcmd_observables, mpcmd_checkpoint, mpcmd_restore, mpcmd_set_cell_order
+  public :: mpcmd_concentration, mpcmd_dimer_axes
   public :: mpcmd_check
 
   interface
@@ -170,6 +178,23 @@ module mpcmd_shim
       import :: c_int, c_ptr, mpcmd_obs
       type(c_ptr), value :: ctx
       type(mpcmd_obs), intent(out) :: obs
+    end function
+    ! output_mod.f95:482-575: totals(4) = TotA, TotB, ConcA, ConcB; the 1D and 2D
+    ! fields in the reference's own array order (concA1d(nx), concA2d_xy(nx,ny) ...)
+    integer(c_int) function mpcmd_concentration(ctx, p, totals, c1d_a, c1d_b, xy_a, xy_b, xz_a, xz_b, &
+        yz_a, yz_b) bind(C, name="mpcmd_concentration")
+      import :: c_int, c_ptr, c_double, mpcmd_conc_params
+      type(c_ptr), value :: ctx
+      type(mpcmd_conc_params), intent(in) :: p
+      real(c_double), intent(out) :: totals(*), c1d_a(*), c1d_b(*), xy_a(*), xy_b(*)
+      real(c_double), intent(out) :: xz_a(*), xz_b(*), yz_a(*), yz_b(*)
+    end function
+    ! nucvec(3, numdims): output_mod.f95:826-846 with normalize = 0
+    integer(c_int) function mpcmd_dimer_axes(ctx, normalize, nucvec, vdot) bind(C, name="mpcmd_dimer_axes")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: normalize
+      real(c_double), intent(out) :: nucvec(*), vdot(*)
     end function
     integer(c_int) function mpcmd_checkpoint(ctx, path) bind(C, name="mpcmd_checkpoint")
       import :: c_int, c_ptr, c_char

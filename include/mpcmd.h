@@ -130,6 +130,36 @@ int mpcmd_observables(mpcmd_ctx* ctx, mpcmd_obs* out);  /* output_mod.f95:681-80
 int mpcmd_checkpoint(mpcmd_ctx* ctx, const char* path); /* restart_mod.f95 state    */
 int mpcmd_restore(mpcmd_ctx* ctx, const char* path);
 
+/* Concentration fields (output_mod.f95:482-575): species A (code 0) and B
+ * (code 1) counted in slabs of half thickness `half_width` (the reference
+ * passes cutoffC) around x_slab / y_slab / z_slab, on bins of x_width,
+ * y_width, z_width.  A particle at coordinate u is in bin ceiling(u / width)
+ * (1-based; a coordinate of exactly 0 goes to bin 1, where the reference
+ * would index 0), and in a slab when |u - slab| <= half_width.  Counts are
+ * divided by the bin volumes of the reference.  Positions are the host view
+ * of mpcmd_download_state (outside particles at the last rebuild).  Outputs
+ * (any may be NULL), nx = int(lx / x_width), ny, nz likewise, 2D arrays with
+ * their first index fastest (Fortran order):
+ *   totals[4]  TotA, TotB, ConcA = TotA / volume, ConcB
+ *   c1d_a/b    [nx]      z slab, binned along x
+ *   xy_a/b     [nx*ny]   z slab
+ *   xz_a/b     [nx*nz]   y slab
+ *   yz_a/b     [ny*nz]   x slab */
+typedef struct mpcmd_conc_params {
+  double x_slab, y_slab, z_slab;
+  double half_width;
+  double x_width, y_width, z_width;
+} mpcmd_conc_params;
+int mpcmd_concentration(mpcmd_ctx* ctx, const mpcmd_conc_params* p, double* totals,
+                        double* c1d_a, double* c1d_b, double* xy_a, double* xy_b,
+                        double* xz_a, double* xz_b, double* yz_a, double* yz_b);
+/* Dimer axes: d = X_C - X_N with the minimum image on the periodic axes,
+ * nucvec[3k..3k+2] = d / Dcn when normalize == 0 (output_mod.f95:826-846) or
+ * d / |d| when normalize == 1 (Output_SelkovDimer.f90:146-166); vdot[k] (may
+ * be NULL) = centre-of-mass velocity . unit axis, the propulsion speed of
+ * Output_SelkovDimer.f90:168-172. */
+int mpcmd_dimer_axes(mpcmd_ctx* ctx, int normalize, double* nucvec, double* vdot);
+
 /* Inspection (parity tests) -------------------------------------------- */
 int mpcmd_get_new_cell(mpcmd_ctx* ctx, int64_t* newcell);           /* NewCellN     */
 int mpcmd_get_cell_rotation(mpcmd_ctx* ctx, double* cm, double* axis, int32_t* count);

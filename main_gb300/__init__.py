@@ -32,6 +32,12 @@ class MpcmdError(RuntimeError):
         super().__init__("mpcmd %s failed: %s (%d)" % (what, STATUS.get(status, "?"), status))
 
 
+class MpcmdConcParams(C.Structure):
+    _fields_ = [("x_slab", C.c_double), ("y_slab", C.c_double), ("z_slab", C.c_double),
+                ("half_width", C.c_double), ("x_width", C.c_double), ("y_width", C.c_double),
+                ("z_width", C.c_double)]
+
+
 class MpcmdObs(C.Structure):
     _fields_ = [
         ("momentum", C.c_double * 3), ("solvent_momentum", C.c_double * 3), ("kinetic_solvent", C.c_double),
@@ -68,6 +74,8 @@ SIGNATURES = {
     "mpcmd_mpc_rotation": (C.c_int, [_P]),
     "mpcmd_reaction": (C.c_int, [_P]),
     "mpcmd_observables": (C.c_int, [_P, C.POINTER(MpcmdObs)]),
+    "mpcmd_concentration": (C.c_int, [_P, C.POINTER(MpcmdConcParams)] + [_dp] * 9),
+    "mpcmd_dimer_axes": (C.c_int, [_P, C.c_int, _dp, _dp]),
     "mpcmd_checkpoint": (C.c_int, [_P, C.c_char_p]),
     "mpcmd_restore": (C.c_int, [_P, C.c_char_p]),
     "mpcmd_get_new_cell": (C.c_int, [_P, _lp]),
@@ -237,6 +245,31 @@ class Engine:
             "species_count": np.array(o.species_count[:]), "n_inside": o.n_inside,
             "time_count": o.time_count, "time_penetrate": o.time_penetrate, "cstep": o.cstep,
         }
+
+    def concentration(self, x_slab, y_slab, z_slab, half_width, x_width=0.5, y_width=0.5, z_width=0.5):
+        """Concentration fields of species A (0) and B (1), output_mod.f95:482-575:
+        totals (TotA, TotB, ConcA, ConcB) and the 1D / 2D slab fields (2D arrays
+        shaped (n_first, n_second) with the first index the reference's first)."""
+        prm = MpcmdConcParams(x_slab, y_slab, z_slab, half_width, x_width, y_width, z_width)
+        L = (self.cfg["lx"], self.cfg["ly"], self.cfg["lz"])
+        nx, ny, nz = (int(L[c] / w) if w > 0 else 0 for c, w in enumerate((x_width, y_width, z_width)))
+        out = {"totals": np.zeros(4), "c1d_a": np.zeros(nx), "c1d_b": np.zeros(nx),
+               "xy_a": np.zeros(nx * ny), "xy_b": np.zeros(nx * ny), "xz_a": np.zeros(nx * nz),
+               "xz_b": np.zeros(nx * nz), "yz_a": np.zeros(ny * nz), "yz_b": np.zeros(ny * nz)}
+        keys = ("totals", "c1d_a", "c1d_b", "xy_a", "xy_b", "xz_a", "xz_b", "yz_a", "yz_b")
+        self._c(lib().mpcmd_concentration(self.h, C.byref(prm), *[_ptr(out[k], C.c_double) for k in keys]),
+                "concentration")
+        return out
+
+    def dimer_axes(self, normalize=0):
+        """(nucvec [n_dimers, 3], propulsion speed [n_dimers]); normalize 0 divides
+        by Dcn (output_mod.f95:826-846), 1 by |d| (Output_SelkovDimer.f90:146-172)."""
+        nd = self.cfg["n_dimers"]
+        nuc = np.zeros((max(nd, 1), 3))
+        vd = np.zeros(max(nd, 1))
+        self._c(lib().mpcmd_dimer_axes(self.h, normalize, _ptr(nuc, C.c_double), _ptr(vd, C.c_double)),
+                "dimer_axes")
+        return nuc[:nd], vd[:nd]
 
     # -- inspection ------------------------------------------------------
     def new_cell(self):

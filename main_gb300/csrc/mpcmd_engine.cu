@@ -133,6 +133,8 @@ struct EngineBase {
   virtual int rotation_stage() = 0;
   virtual int reaction_stage() = 0;
   virtual int observables(mpcmd_obs* o) = 0;
+  virtual int concentration(const mpcmd_conc_params* p, double* totals, double* const* fields) = 0;
+  virtual int dimer_axes(int normalize, double* nucvec, double* vdot) = 0;
   virtual int get_new_cell(int64_t* out) = 0;
   virtual int get_cell_rotation(double* cm, double* axis, int32_t* count) = 0;
   virtual int get_distribute(int32_t* counts, int64_t* first) = 0;
@@ -869,6 +871,103 @@ struct Engine : EngineBase {
     return dev_status_to_api(h.status);
   }
 
+  // output_mod.f95:482-575 on the device: a flush of the shell, one counting
+  // pass over the particles, normalisation on the host.  Allocates its count
+  // arrays per call (an output-cadence call, not part of the step).
+  int concentration(const mpcmd_conc_params* p, double* totals, double* const* fields) override {
+    if (!(p->x_width > 0 && p->y_width > 0 && p->z_width > 0 && p->half_width >= 0)) return MPCMD_ERR_CONFIG;
+    const double L[3] = {(double)cfg.lx, (double)cfg.ly, (double)cfg.lz};
+    const int64_t nx = (int64_t)(L[0] / p->x_width), ny = (int64_t)(L[1] / p->y_width), nz = (int64_t)(L[2] / p->z_width);
+    if (nx < 1 || ny < 1 || nz < 1 || nx > (1 << 20) || ny > (1 << 20) || nz > (1 << 20)) return MPCMD_ERR_CONFIG;
+    if (nx * ny > (int64_t)1 << 28 || nx * nz > (int64_t)1 << 28 || ny * nz > (int64_t)1 << 28) return MPCMD_ERR_CONFIG;
+    if (advanced) return MPCMD_ERR_STATE;
+    flush_shell();
+    const int64_t sz[8] = {nx, nx, nx * ny, nx * ny, nx * nz, nx * nz, ny * nz, ny * nz};
+    int64_t off[9];
+    off[0] = 0;
+    for (int q = 0; q < 8; ++q) off[q + 1] = off[q] + sz[q];
+    uint32_t* cnt = nullptr;
+    unsigned long long* tot = nullptr;
+    if (cudaMalloc(&cnt, sizeof(uint32_t) * (size_t)off[8]) != cudaSuccess) return MPCMD_ERR_CUDA;
+    if (cudaMalloc(&tot, 2 * sizeof(unsigned long long)) != cudaSuccess) { cudaFree(cnt); return MPCMD_ERR_CUDA; }
+    int r = MPCMD_OK;
+    std::vector<uint32_t> h((size_t)off[8]);
+    unsigned long long ht[2] = {0, 0};
+    ConcArgs c;
+    c.xs = p->x_slab; c.ys = p->y_slab; c.zs = p->z_slab; c.hw = p->half_width;
+    c.xw = p->x_width; c.yw = p->y_width; c.zw = p->z_width;
+    c.nx = (int)nx; c.ny = (int)ny; c.nz = (int)nz;
+    uint32_t* ptrs[8];
+    for (int q = 0; q < 8; ++q) ptrs[q] = cnt + off[q];
+    c.c1a = ptrs[0]; c.c1b = ptrs[1]; c.xya = ptrs[2]; c.xyb = ptrs[3];
+    c.xza = ptrs[4]; c.xzb = ptrs[5]; c.yza = ptrs[6]; c.yzb = ptrs[7];
+    c.tot = tot;
+    if (cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (size_t)off[8], st) != cudaSuccess ||
+        cudaMemsetAsync(tot, 0, 2 * sizeof(unsigned long long), st) != cudaSuccess) {
+      r = MPCMD_ERR_CUDA;
+    } else {
+      Launch<T>::concentration(d, kp, time_count, (int)(last_rebuild - last_full), c, st);
+      if (cudaMemcpyAsync(h.data(), cnt, sizeof(uint32_t) * h.size(), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaMemcpyAsync(ht, tot, sizeof(ht), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        r = MPCMD_ERR_CUDA;
+    }
+    cudaFree(cnt);
+    cudaFree(tot);
+    if (r) return r;
+    const double hw2 = 2.0 * p->half_width;
+    const double vol = (double)(int64_t)(L[0] * L[1] * L[2]);
+    const double v[8] = {p->x_width * L[1] * hw2, p->x_width * L[1] * hw2,
+                         p->x_width * p->y_width * hw2, p->x_width * p->y_width * hw2,
+                         p->x_width * p->z_width * hw2, p->x_width * p->z_width * hw2,
+                         p->y_width * p->z_width * hw2, p->y_width * p->z_width * hw2};
+    if (totals) {
+      totals[0] = (double)ht[0]; totals[1] = (double)ht[1];
+      totals[2] = (double)ht[0] / vol; totals[3] = (double)ht[1] / vol;
+    }
+    for (int q = 0; q < 8; ++q) {
+      if (!fields[q]) continue;
+      for (int64_t j = 0; j < sz[q]; ++j) fields[q][j] = (double)h[(size_t)(off[q] + j)] / v[q];
+    }
+    return check_device_status();
+  }
+
+  // Dimer axes from the FP64 sphere state: output_mod.f95:826-846 (d / Dcn)
+  // or Output_SelkovDimer.f90:146-172 (unit vector, propulsion speed).
+  int dimer_axes(int normalize, double* nucvec, double* vdot) override {
+    if (normalize != 0 && normalize != 1) return MPCMD_ERR_CONFIG;
+    if (kp.nd == 0) return MPCMD_OK;
+    std::vector<double> X(3 * (size_t)kp.ns), V(3 * (size_t)kp.ns);
+    CK(cudaMemcpyAsync(X.data(), d.dpos, X.size() * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(V.data(), d.dvel, V.size() * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const double L[3] = {(double)cfg.lx, (double)cfg.ly, (double)cfg.lz};
+    const bool per[3] = {true, true, cfg.geometry == MPCMD_GEOM_PERIODIC};
+    for (int k = 0; k < kp.nd; ++k) {
+      double dd[3];
+      for (int c = 0; c < 3; ++c) {
+        dd[c] = X[6 * (size_t)k + c] - X[6 * (size_t)k + 3 + c];
+        if (per[c]) {
+          if (dd[c] > 0.5 * L[c]) dd[c] -= L[c];
+          else if (dd[c] < -0.5 * L[c]) dd[c] += L[c];
+        }
+      }
+      const double len = std::sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+      const double den = normalize ? len : cfg.dcn;
+      if (nucvec)
+        for (int c = 0; c < 3; ++c) nucvec[3 * (size_t)k + c] = dd[c] / den;
+      if (vdot) {
+        double s = 0.0;
+        for (int c = 0; c < 3; ++c) {
+          const double vcm = (cfg.mc * V[6 * (size_t)k + c] + cfg.mn * V[6 * (size_t)k + 3 + c]) / (cfg.mn + cfg.mc);
+          s += vcm * (dd[c] / len);
+        }
+        vdot[k] = s;
+      }
+    }
+    return MPCMD_OK;
+  }
+
   int get_new_cell(int64_t* out) override {
     std::vector<uint32_t> k((size_t)kp.n);
     CK(cudaMemcpy(k.data(), d.skey, k.size() * 4, cudaMemcpyDeviceToHost));
@@ -1179,6 +1278,18 @@ int mpcmd_observables(mpcmd_ctx* ctx, mpcmd_obs* out) {
   CTX_OK(ctx);
   if (!out) return MPCMD_ERR_CONFIG;
   return ctx->e->observables(out);
+}
+int mpcmd_concentration(mpcmd_ctx* ctx, const mpcmd_conc_params* p, double* totals, double* c1d_a,
+                        double* c1d_b, double* xy_a, double* xy_b, double* xz_a, double* xz_b, double* yz_a,
+                        double* yz_b) {
+  CTX_OK(ctx);
+  if (!p) return MPCMD_ERR_CONFIG;
+  double* const fields[8] = {c1d_a, c1d_b, xy_a, xy_b, xz_a, xz_b, yz_a, yz_b};
+  return ctx->e->concentration(p, totals, fields);
+}
+int mpcmd_dimer_axes(mpcmd_ctx* ctx, int normalize, double* nucvec, double* vdot) {
+  CTX_OK(ctx);
+  return ctx->e->dimer_axes(normalize, nucvec, vdot);
 }
 int mpcmd_checkpoint(mpcmd_ctx* ctx, const char* path) {
   CTX_OK(ctx);

@@ -80,6 +80,15 @@ struct Particles {
   uint8_t* flag;
 };
 
+// Concentration-field counting (mpcmd_concentration): slab centres, half
+// thickness, bin widths, bin counts per axis and the device count arrays.
+struct ConcArgs {
+  double xs, ys, zs, hw, xw, yw, zw;
+  int nx, ny, nz;
+  uint32_t *c1a, *c1b, *xya, *xyb, *xza, *xzb, *yza, *yzb;
+  unsigned long long* tot;   // [2] particles of species 0 and 1
+};
+
 template <typename T>
 struct Dev {
   Particles<T> p;          // main home, reference index order
@@ -172,6 +181,8 @@ struct Launch {
   static void regather(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, cudaStream_t st);
+  static void concentration(const Dev<T>& d, const KParams<T>& kp, int tc, int tc_defer, const ConcArgs& c,
+                            cudaStream_t st);
   // resident blocks per SM of the persistent kernels (rebuild, force, rotate)
   static void occupancy(int* blocks);
   static void init_solvent(const Dev<T>& d, const KParams<T>& kp, const int64_t* bounds, double kT,

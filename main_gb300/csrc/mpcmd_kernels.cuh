@@ -251,6 +251,68 @@ void Launch<T>::download_convert(const Dev<T>& d, const KParams<T>& kp, double* 
   LAUNCH_COUNT();
 }
 
+// Concentration fields (output_mod.f95:482-575) on the host view of the
+// positions (the k_download reconstruction): counts of species 0 and 1 per
+// bin of the three slabs, and the box totals (one atomic per block).
+__device__ __forceinline__ int conc_bin(double u, double w, int nb) {
+  int j = (int)ceil(u / w);
+  j = j < 1 ? 1 : (j > nb ? nb : j);
+  return j - 1;
+}
+
+template <typename T>
+__global__ void k_concentration(Particles<T> p, KParams<T> kp, const uint8_t* react_box, int tc, int tc_defer,
+                                ConcArgs c) {
+  __shared__ unsigned int blk[2];
+  if (threadIdx.x < 2) blk[threadIdx.x] = 0u;
+  __syncthreads();
+  unsigned int na = 0u, nb = 0u;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    const uint8_t f = p.flag[i];
+    const int sp = f & FLAG_SPECIES;
+    if (sp > 1) continue;
+    uint32_t cl = p.cell[i];
+    T ox = p.ox[i], oy = p.oy[i], oz = p.oz[i];
+    int lag = 0;
+    if (f & FLAG_PASSIVE) lag = tc;
+    else if (!(f & (FLAG_INLIST | FLAG_FRESH | FLAG_HOME_SHELL))) lag = tc_defer;
+    if (lag > 0) {
+      T vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
+      uint8_t ff = f;
+      stream_one(kp, react_box, cl, ox, oy, oz, vx, vy, vz, ff, true, lag);
+    }
+    const double x = (double)cell_x(cl) + (double)ox;
+    const double y = (double)cell_y(cl) + (double)oy;
+    const double z = (double)cell_z(cl) + (double)oz;
+    if (sp == 0) ++na; else ++nb;
+    if (z <= c.zs + c.hw && z >= c.zs - c.hw) {
+      const int j = conc_bin(x, c.xw, c.nx), k = conc_bin(y, c.yw, c.ny);
+      atomicAdd(sp == 0 ? &c.c1a[j] : &c.c1b[j], 1u);
+      atomicAdd(sp == 0 ? &c.xya[j + (size_t)c.nx * k] : &c.xyb[j + (size_t)c.nx * k], 1u);
+    }
+    if (y <= c.ys + c.hw && y >= c.ys - c.hw) {
+      const int j = conc_bin(x, c.xw, c.nx), k = conc_bin(z, c.zw, c.nz);
+      atomicAdd(sp == 0 ? &c.xza[j + (size_t)c.nx * k] : &c.xzb[j + (size_t)c.nx * k], 1u);
+    }
+    if (x <= c.xs + c.hw && x >= c.xs - c.hw) {
+      const int j = conc_bin(y, c.yw, c.ny), k = conc_bin(z, c.zw, c.nz);
+      atomicAdd(sp == 0 ? &c.yza[j + (size_t)c.ny * k] : &c.yzb[j + (size_t)c.ny * k], 1u);
+    }
+  }
+  atomicAdd(&blk[0], na);
+  atomicAdd(&blk[1], nb);
+  __syncthreads();
+  if (threadIdx.x < 2) atomicAdd(&c.tot[threadIdx.x], (unsigned long long)blk[threadIdx.x]);
+}
+
+template <typename T>
+void Launch<T>::concentration(const Dev<T>& d, const KParams<T>& kp, int tc, int tc_defer, const ConcArgs& c,
+                              cudaStream_t st) {
+  k_concentration<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, tc, tc_defer, c);
+  LAUNCH_COUNT();
+}
+
 template <typename T>
 __global__ void k_download_flag(Particles<T> p, KParams<T> kp, int32_t* out) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;

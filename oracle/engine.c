@@ -1230,3 +1230,80 @@ int orc_observables(const orc_t* o, orc_obs* out) {
   out->cstep = o->cstep;
   return ORC_OK;
 }
+
+/* ------------------------------------------------- concentration fields -- */
+/* output_mod.f95:482-575: TotA/TotB over the whole box, then A and B counted
+ * in a z slab (1D along x, 2D in x-y), a y slab (x-z) and an x slab (y-z) of
+ * half thickness prm[3] around prm[0..2], bin = ceiling(u / width), divided
+ * by the bin volume.  A coordinate of exactly 0 (bin 0 in the reference,
+ * outside its arrays) is counted in bin 1; indices above the last bin are
+ * clamped to it. */
+static int64_t conc_bin(double u, double w, int64_t nb) {
+  int64_t j = (int64_t)ceil(u / w);
+  if (j < 1) j = 1;
+  if (j > nb) j = nb;
+  return j - 1;
+}
+
+int orc_concentration(int64_t n, const double* x, const double* y, const double* z,
+                      const int32_t* flag, const double* box, const double* prm, double* totals,
+                      double* c1d_a, double* c1d_b, double* xy_a, double* xy_b,
+                      double* xz_a, double* xz_b, double* yz_a, double* yz_b) {
+  const double xs = prm[0], ys = prm[1], zs = prm[2], hw = prm[3];
+  const double xw = prm[4], yw = prm[5], zw = prm[6];
+  if (!(xw > 0 && yw > 0 && zw > 0 && hw >= 0)) return ORC_ERR_CONFIG;
+  const int64_t nx = (int64_t)(box[0] / xw), ny = (int64_t)(box[1] / yw), nz = (int64_t)(box[2] / zw);
+  if (nx < 1 || ny < 1 || nz < 1) return ORC_ERR_CONFIG;
+  double* a1 = calloc((size_t)nx, sizeof(double));
+  double* b1 = calloc((size_t)nx, sizeof(double));
+  double* axy = calloc((size_t)(nx * ny), sizeof(double));
+  double* bxy = calloc((size_t)(nx * ny), sizeof(double));
+  double* axz = calloc((size_t)(nx * nz), sizeof(double));
+  double* bxz = calloc((size_t)(nx * nz), sizeof(double));
+  double* ayz = calloc((size_t)(ny * nz), sizeof(double));
+  double* byz = calloc((size_t)(ny * nz), sizeof(double));
+  if (!a1 || !b1 || !axy || !bxy || !axz || !bxz || !ayz || !byz) {
+    free(a1); free(b1); free(axy); free(bxy); free(axz); free(bxz); free(ayz); free(byz);
+    return ORC_ERR_ALLOC;
+  }
+  double tota = 0, totb = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t f = flag[i];
+    if (f != 0 && f != 1) continue;
+    if (f == 0) tota += 1.; else totb += 1.;
+    if (z[i] <= zs + hw && z[i] >= zs - hw) {
+      const int64_t j = conc_bin(x[i], xw, nx), k = conc_bin(y[i], yw, ny);
+      if (f == 0) { a1[j] += 1.; axy[j + nx * k] += 1.; } else { b1[j] += 1.; bxy[j + nx * k] += 1.; }
+    }
+    if (y[i] <= ys + hw && y[i] >= ys - hw) {
+      const int64_t j = conc_bin(x[i], xw, nx), k = conc_bin(z[i], zw, nz);
+      if (f == 0) axz[j + nx * k] += 1.; else bxz[j + nx * k] += 1.;
+    }
+    if (x[i] <= xs + hw && x[i] >= xs - hw) {
+      const int64_t j = conc_bin(y[i], yw, ny), k = conc_bin(z[i], zw, nz);
+      if (f == 0) ayz[j + ny * k] += 1.; else byz[j + ny * k] += 1.;
+    }
+  }
+  const double vol = (double)(int64_t)(box[0] * box[1] * box[2]);
+  const double v1 = xw * box[1] * (2. * hw), vxy = xw * yw * (2. * hw);
+  const double vxz = xw * zw * (2. * hw), vyz = yw * zw * (2. * hw);
+  if (totals) { totals[0] = tota; totals[1] = totb; totals[2] = tota / vol; totals[3] = totb / vol; }
+  for (int64_t j = 0; j < nx; ++j) {
+    if (c1d_a) c1d_a[j] = a1[j] / v1;
+    if (c1d_b) c1d_b[j] = b1[j] / v1;
+  }
+  for (int64_t q = 0; q < nx * ny; ++q) {
+    if (xy_a) xy_a[q] = axy[q] / vxy;
+    if (xy_b) xy_b[q] = bxy[q] / vxy;
+  }
+  for (int64_t q = 0; q < nx * nz; ++q) {
+    if (xz_a) xz_a[q] = axz[q] / vxz;
+    if (xz_b) xz_b[q] = bxz[q] / vxz;
+  }
+  for (int64_t q = 0; q < ny * nz; ++q) {
+    if (yz_a) yz_a[q] = ayz[q] / vyz;
+    if (yz_b) yz_b[q] = byz[q] / vyz;
+  }
+  free(a1); free(b1); free(axy); free(bxy); free(axz); free(bxz); free(ayz); free(byz);
+  return ORC_OK;
+}

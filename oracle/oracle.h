@@ -126,6 +126,13 @@ int orc_selkov_step(orc_t* o);
 
 /* Inspection. */
 int orc_observables(const orc_t* o, orc_obs* out);
+/* Concentration fields of species 0 and 1 (output_mod.f95:482-575) from host
+ * arrays: box[3]; prm = x_slab, y_slab, z_slab, half_width, x_width, y_width,
+ * z_width; outputs as mpcmd_concentration (any may be NULL). */
+int orc_concentration(int64_t n, const double* x, const double* y, const double* z,
+                      const int32_t* flag, const double* box, const double* prm, double* totals,
+                      double* c1d_a, double* c1d_b, double* xy_a, double* xy_b,
+                      double* xz_a, double* xz_b, double* yz_a, double* yz_b);
 int64_t orc_n_cells_shifted(const orc_t* o);
 int orc_get_new_cell(const orc_t* o, int64_t* newcell);
 int orc_get_cell_rotation(const orc_t* o, double* cm, double* axis, int32_t* count);

@@ -71,6 +71,7 @@ def lib():
             "orc_reaction": (C.c_int, [P]),
             "orc_selkov_prepare": (C.c_int, [P]), "orc_selkov_step": (C.c_int, [P]),
             "orc_observables": (C.c_int, [P, C.POINTER(OrcObs)]),
+            "orc_concentration": (C.c_int, [C.c_int64, dp, dp, dp, ip, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]),
             "orc_n_cells_shifted": (C.c_int64, [P]),
             "orc_get_new_cell": (C.c_int, [P, lp]),
             "orc_get_cell_rotation": (C.c_int, [P, dp, dp, ip]),
@@ -318,3 +319,28 @@ class Oracle:
         t = np.zeros(int(self.cfg["lx"]) * int(self.cfg["ly"]), dtype=np.int32)
         lib().orc_reactive_grid_table(self.h, _ptr(t, C.c_int32))
         return t
+
+
+def concentration(x, y, z, flag, box, prm):
+    """Concentration fields (output_mod.f95:482-575) of host arrays: box
+    (Lx, Ly, Lz), prm = (x_slab, y_slab, z_slab, half_width, x_width, y_width,
+    z_width).  Returns totals[4] and the 1D / 2D fields (2D in Fortran order,
+    first index fastest)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    flag = np.ascontiguousarray(flag, dtype=np.int32)
+    box = np.ascontiguousarray(box, dtype=np.float64)
+    prm = np.ascontiguousarray(prm, dtype=np.float64)
+    nx, ny, nz = (int(box[c] / prm[4 + c]) if prm[4 + c] > 0 else 0 for c in range(3))
+    out = {"totals": np.zeros(4), "c1d_a": np.zeros(nx), "c1d_b": np.zeros(nx),
+           "xy_a": np.zeros(nx * ny), "xy_b": np.zeros(nx * ny), "xz_a": np.zeros(nx * nz),
+           "xz_b": np.zeros(nx * nz), "yz_a": np.zeros(ny * nz), "yz_b": np.zeros(ny * nz)}
+    dp = C.c_double
+    st = lib().orc_concentration(len(x), _ptr(x, dp), _ptr(y, dp), _ptr(z, dp), _ptr(flag, C.c_int32),
+                                 _ptr(box, dp), _ptr(prm, dp),
+                                 *[_ptr(out[k], dp) for k in ("totals", "c1d_a", "c1d_b", "xy_a", "xy_b",
+                                                              "xz_a", "xz_b", "yz_a", "yz_b")])
+    if st != 0:
+        raise RuntimeError("orc_concentration failed (%d)" % st)
+    return out
