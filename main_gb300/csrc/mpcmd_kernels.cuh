@@ -1351,11 +1351,146 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
   if (iters) atomicAdd(&d.ctr->rattle_iters, iters);
 }
 
+// Sum over the four lanes of a dimer's group (mask: those lanes, which
+// always take the same branches); every lane gets the same bits (the
+// butterfly adds the same pairs in every lane).
+__device__ __forceinline__ double group4_sum(unsigned mask, double v) {
+  v += __shfl_xor_sync(mask, v, 1);
+  v += __shfl_xor_sync(mask, v, 2);
+  return v;
+}
+
+// The FP32 build's dimer step with the three Cartesian components of a dimer
+// on three lanes of a 4-lane group (the fourth holds zeros and the energy):
+// the same update as k_dimer's fast path (totals, RATTLE velocities, RATTLE
+// positions, single-shift wrap), with the constraint dot products summed
+// across the group.  On this part FP64 instructions are issued at a few lanes
+// per SM cycle, so the per-dimer chain of FP64 instructions, not the lane
+// count, sets the time; splitting the components shortens that chain about
+// threefold.  The FP64 parity build keeps k_dimer and the oracle's order.
+template <typename T>
+__global__ void k_dimer_split(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3, int rattle_max) {
+  if (d.ctr->abort_step) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = t >> 2, c = t & 3;
+  const unsigned gmask = 0xFu << (threadIdx.x & 28);   // this group's four lanes
+  const bool live = k < kp.nd;        // the whole 4-lane group agrees
+  const int kk = live ? k : 0;
+  const bool comp = c < 3;
+  const double dt = kp.dtd, Dcn = kp.dcn;
+  const double hIMc = kp.hIMc, hIMn = kp.hIMn, IIM = kp.IIM;
+  const double iMc = kp.iMc, iMn = kp.iMn, iD2 = kp.iD2, iMcdt = kp.iMcdt, iMndt = kp.iMndt;
+  const bool per = kp.geometry == 1;
+  const int cc = comp ? c : 0;
+  const bool wrapc = comp && (c < 2 || per);
+  const double L = kp.Ld[cc];
+  const int s1 = 2 * kk, s2 = 2 * kk + 1;
+  double X1 = 0, X2 = 0, V1 = 0, V2 = 0, F1 = 0, F2 = 0, Q1 = 0, Q2 = 0;
+  if (live && comp) {
+    X1 = d.dpos[3 * s1 + c]; X2 = d.dpos[3 * s2 + c];
+    V1 = d.dvel[3 * s1 + c]; V2 = d.dvel[3 * s2 + c];
+    F1 = d.dfrc[3 * s1 + c]; F2 = d.dfrc[3 * s2 + c];
+    Q1 = d.dq[3 * s1 + c]; Q2 = d.dq[3 * s2 + c];
+  }
+  unsigned long long iters = 0;
+  if (mode & 1) {
+    double fw1 = 0., pw1 = 0., fw2 = 0., pw2 = 0.;
+    if (live && c == 2 && !per) {
+      lj_wall(kp, X1, kp.rwc, w3, fw1, pw1);
+      lj_wall(kp, X2, kp.rwn, w3, fw2, pw2);
+    }
+    // the wall energies travel from the z lane to the energy lane
+    const int zl = (threadIdx.x & 31 & ~3) | 2;
+    const double p1 = __shfl_sync(gmask, pw1, zl), p2 = __shfl_sync(gmask, pw2, zl);
+    if (live) {
+      const int q = comp ? c : 3;
+      const double a1 = d.facc[4 * s1 + q] + d.fmot[4 * s1 + q];
+      const double a2 = d.facc[4 * s2 + q] + d.fmot[4 * s2 + q];
+      d.facc[4 * s1 + q] = 0.; d.facc[4 * s2 + q] = 0.;
+      if (comp) {
+        F1 = a1 + (c == 2 ? fw1 : 0.);
+        F2 = a2 + (c == 2 ? fw2 : 0.);
+      } else {
+        d.dpot[kk] = (a1 + p1) + (a2 + p2);
+      }
+    }
+    if (comp) { V1 = Q1 + hIMc * F1; V2 = Q2 + hIMn * F2; }
+    int acc = 0;
+    for (;;) {
+      double dd = X1 - X2;
+      if (wrapc) dd = dmin_image(dd, L);
+      const double Con2diff = 2.0 * group4_sum(gmask, (V1 - V2) * dd);
+      if (!live || fabs(Con2diff) < 1.e-8) break;
+      if (acc == rattle_max) { if (c == 0) atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      const double O2 = -(0.5 * (IIM * Con2diff) * iD2);
+      V1 = V1 + O2 * dd * iMc;
+      V2 = V2 - O2 * dd * iMn;
+      acc++;
+    }
+    iters += acc;
+    if (live && comp) {
+      d.dvel[3 * s1 + c] = V1; d.dvel[3 * s2 + c] = V2;
+      d.dfrc[3 * s1 + c] = F1; d.dfrc[3 * s2 + c] = F2;
+    }
+  }
+  if (mode & 2) {
+    const double pr1 = X1, pr2 = X2;
+    double dP = X1 - X2;
+    if (wrapc) dP = dmin_image(dP, L);
+    if (!comp) dP = 0.;
+    Q1 = V1 + hIMc * F1; Q2 = V2 + hIMn * F2;
+    X1 = X1 + dt * Q1; X2 = X2 + dt * Q2;
+    int acc = 0;
+    for (;;) {
+      double dd = X1 - X2;
+      if (wrapc) dd = dmin_image(dd, L);
+      if (!comp) dd = 0.;
+      const double Con1diff = group4_sum(gmask, dd * dd) - Dcn * Dcn;
+      if (!live || fabs(Con1diff) < 1.e-6) break;
+      if (acc == rattle_max) { if (c == 0) atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      const double den = group4_sum(gmask, dd * dP);
+      double r = (double)__frcp_rn((float)den);
+      r = r * (2.0 - den * r);
+      r = r * (2.0 - den * r);
+      const double G2 = 2.0 * (-(0.25 * Con1diff * IIM) * r);
+      X1 = pr1 + Q1 * dt + G2 * dP * iMc;
+      X2 = pr2 + Q2 * dt - G2 * dP * iMn;
+      Q1 = Q1 + G2 * dP * iMcdt;
+      Q2 = Q2 - G2 * dP * iMndt;
+      acc++;
+    }
+    if (wrapc && (c < 2 || per)) {
+      if (X1 >= L) X1 -= L; else if (X1 < 0.0) X1 += L;
+      if (X2 >= L) X2 -= L; else if (X2 < 0.0) X2 += L;
+      if (!(X1 >= 0.0 && X1 < L)) X1 = X1 - L * floor(X1 / L);
+      if (!(X2 >= 0.0 && X2 < L)) X2 = X2 - L * floor(X2 / L);
+    }
+    iters += acc;
+    if (live && comp) {
+      d.dpos[3 * s1 + c] = X1; d.dpos[3 * s2 + c] = X2;
+      d.dq[3 * s1 + c] = Q1; d.dq[3 * s2 + c] = Q2;
+      const double f1 = floor(X1), f2 = floor(X2);
+      SphereRel<T>& r1 = d.srel[s1];
+      SphereRel<T>& r2 = d.srel[s2];
+      if (c == 0) { r1.cx = (int)f1; r1.ox = (T)(X1 - f1); r2.cx = (int)f2; r2.ox = (T)(X2 - f2); }
+      else if (c == 1) { r1.cy = (int)f1; r1.oy = (T)(X1 - f1); r2.cy = (int)f2; r2.oy = (T)(X2 - f2); }
+      else { r1.cz = (int)f1; r1.oz = (T)(X1 - f1); r2.cz = (int)f2; r2.oz = (T)(X2 - f2); }
+    }
+  }
+  if (live && c == 0 && iters) atomicAdd(&d.ctr->rattle_iters, iters);
+}
+
 template <typename T>
 void Launch<T>::dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode, double w3,
                       int rattle_max, cudaStream_t st) {
   if (kp.nd == 0) return;
-  k_dimer<T><<<(kp.nd + 63) / 64, 64, 0, st>>>(d, kp, a, mode, w3, rattle_max);
+  if (sizeof(T) == 4) {
+    // four lanes per dimer, one 32-lane block per eight dimers (spread over the SMs)
+    const int threads = 4 * kp.nd;
+    k_dimer_split<T><<<(threads + 31) / 32, 32, 0, st>>>(d, kp, a, mode, w3, rattle_max);
+  } else {
+    k_dimer<T><<<(kp.nd + 63) / 64, 64, 0, st>>>(d, kp, a, mode, w3, rattle_max);
+  }
   LAUNCH_COUNT();
 }
 
