@@ -77,13 +77,14 @@ MPCMD_HD void contract_bits(uint64_t seed, uint32_t tag, uint32_t index, uint32_
   m1 = ((uint64_t)c2 << 21) | (uint64_t)(c3 >> 11);
 }
 
-// Leading 32-bit word of draw `which` (0: words 0-1, 1: words 2-3): the top
-// bits of the 53-bit uniform of contract_pair.
-MPCMD_HD uint32_t index_word(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
-                             uint32_t step, int which) {
+// Leading 32-bit words of both draws of one counter (one Philox evaluation):
+// w0 the top bits of contract_pair's u0, w2 those of u1.
+MPCMD_HD void contract_words(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
+                             uint32_t step, uint32_t& w0, uint32_t& w2) {
   uint32_t c0 = index, c1 = extra, c2 = step, c3 = tag;
   philox4x32_10(c0, c1, c2, c3, (uint32_t)seed, (uint32_t)(seed >> 32));
-  return which ? c2 : c0;
+  w0 = c0;
+  w2 = c2;
 }
 
 // Integer threshold of a probability p for draws compared as `p > u`:
@@ -126,6 +127,7 @@ struct KParams {
   uint64_t thr_ab, thr_ba;   // integer thresholds of rp_ab / rp_ba on the 53-bit draws
   double tau;            // MPC interval
   double k[6];
+  float kf[6], tauf;      // the same rounded to float (FP32 reaction path)
   double dtd;            // MD step in FP64
   int nbx, nby, nbz;     // coarse sphere-bin grid
   // dimer constants (FP64): sphere-sphere LJ by pair type [CC, CN, NN]

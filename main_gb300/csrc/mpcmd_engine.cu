@@ -318,7 +318,8 @@ struct Engine : EngineBase {
     kp.thr_ab = prob_threshold(c.rp_ab);
     kp.thr_ba = prob_threshold(c.rp_ba);
     kp.tau = c.mpc_dt;
-    for (int q = 0; q < 6; ++q) kp.k[q] = c.k[q];
+    for (int q = 0; q < 6; ++q) { kp.k[q] = c.k[q]; kp.kf[q] = (float)c.k[q]; }
+    kp.tauf = (float)c.mpc_dt;
     kp.nbx = (c.lx + BIN_EDGE - 1) / BIN_EDGE;
     kp.nby = (c.ly + BIN_EDGE - 1) / BIN_EDGE;
     kp.nbz = (c.lz + BIN_EDGE - 1) / BIN_EDGE;

@@ -1614,21 +1614,22 @@ static __device__ int selkov_channel_fp64(const double* k, double tau, int nF, i
 }
 
 // The same decision in FP32 with a guard band; returns -1 when any comparison
-// is too close to call in FP32 (the caller then uses the FP64 path).
-static __device__ int selkov_channel_fp32(const double* kd, float tau, int nF, int nG, int nI, double x1d, double x2d) {
-  float k0 = (float)kd[0], k1 = (float)kd[1], k2 = (float)kd[2], k3 = (float)kd[3], k4 = (float)kd[4], k5 = (float)kd[5];
+// is too close to call in FP32 (the caller then uses the FP64 path).  The
+// uniforms come in as floats of the leading 32 bits of the draws (within
+// 1e-7 of the 53-bit values, far inside the band).
+static __device__ int selkov_channel_fp32(const float* kf, float tau, int nF, int nG, int nI, float x1, float x2) {
+  const float k0 = kf[0], k1 = kf[1], k2 = kf[2], k3 = kf[3], k4 = kf[4], k5 = kf[5];
   float a1 = k0, a2 = k1 * (float)nF, a5 = k4 * (float)nG, a6 = k5;
   float a3 = (nG == 0) ? 0.f : k2 * (float)nF * (float)nG * (float)(nG - 1);
   float a4 = (nG <= 1) ? 0.f : k3 * (float)nG * (float)(nG - 1) * (float)(nG - 2);
   if (nI == 0) { a1 = 0.f; a6 = 0.f; }
   float a00 = a1 + a2 + a3 + a4 + a5 + a6;
   float prob = 1.f - expf(-a00 * tau);
-  float x2 = (float)x2d;
   float gap = prob - x2;
   if (fabsf(gap) < 4e-6f) return -1;
   if (!(gap > 0.f)) return 0;
   if (nI == 0 && nF == 0 && nG == 0) return 0;
-  float a0rand = a00 * (float)x1d;
+  float a0rand = a00 * x1;
   float av[6] = {a1, a2, a3, a4, a5, a6};
   float cum = 0.f;
   const float band = 4e-6f * a00 + 1e-30f;
@@ -1678,8 +1679,8 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
         // FP32 axis from the top 32 bits of each draw; the radius is
         // 2 sqrt(u (1 - u)) = sqrt(1 - theta^2) with both factors at full
         // relative precision (no cancellation near the poles)
-        uint32_t w0 = index_word(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, 0);
-        uint32_t w2 = index_word(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, 1);
+        uint32_t w0, w2;
+        contract_words(kp.seed, TAG_AXIS, (uint32_t)c, 0, a.step, w0, w2);
         const float two32 = 2.3283064365386963e-10f;
         float u1 = (float)w0 * two32;
         float u2 = (float)w2 * two32, v2 = ((float)(~w2) + 1.f) * two32;
@@ -1704,31 +1705,44 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
       uint32_t* fk = d.dfirst + 4 * (size_t)c;
       if (kp.kinetics == 1) {
         int nB = (cnt >> 8) & 255u;
-        double u0, u1;
-        contract_pair(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, u0, u1);
         if (nB > 0) {
-          double a1 = kp.k[0] * (double)nB;
           bool fire;
-          if (sizeof(T) == 4) {
-            float pf = 1.f - expf(-(float)a1 * (float)kp.tau);
-            float g = pf - (float)u0;
-            if (fabsf(g) < 4e-6f) fire = (0. < u0 && u0 <= 1.0 - exp(-a1 * kp.tau));
-            else fire = (0. < u0) && g >= 0.f;
-          } else {
-            double prob1 = 1.0 - exp(-a1 * kp.tau);
-            fire = (0. < u0 && u0 <= prob1);
+          bool exact = sizeof(T) != 4;
+          if (!exact) {
+            // FP32 with a guard band on the leading word of the draw; a call
+            // too close to make (or a zero word) takes the FP64 path
+            uint32_t w0, w2;
+            contract_words(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, w0, w2);
+            const float u0f = (float)w0 * 2.3283064365386963e-10f;
+            const float pf = 1.f - expf(-(kp.kf[0] * (float)nB) * kp.tauf);
+            const float g = pf - u0f;
+            exact = fabsf(g) < 4e-6f || w0 == 0u;
+            fire = g >= 0.f;
+          }
+          if (exact) {
+            double u0, u1;
+            contract_pair(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, u0, u1);
+            const double a1 = kp.k[0] * (double)nB;
+            fire = (0. < u0 && u0 <= 1.0 - exp(-a1 * kp.tau));
           }
           if (fire && fk[1] != 0xFFFFFFFFu) relabel_key(d, fk[1], 0);
         }
       } else if (kp.kinetics == 2 && !d.affected[c]) {
         const int tgt[7] = {-1, 3, 0, 0, 1, 1, 3};
         const int code[7] = {-1, 0, 3, 1, 0, 3, 1};
-        double x1, x2;
-        contract_pair(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, x1, x2);
         int nF = cnt & 255u, nG = (cnt >> 8) & 255u, nI = (cnt >> 24) & 255u;
         int ch = -1;
-        if (sizeof(T) == 4) ch = selkov_channel_fp32(kp.k, (float)kp.tau, nF, nG, nI, x1, x2);
-        if (ch < 0) ch = selkov_channel_fp64(kp.k, kp.tau, nF, nG, nI, x1, x2);
+        if (sizeof(T) == 4) {
+          uint32_t w1, w2;
+          contract_words(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, w1, w2);
+          const float two32 = 2.3283064365386963e-10f;
+          ch = selkov_channel_fp32(kp.kf, kp.tauf, nF, nG, nI, (float)w1 * two32, (float)w2 * two32);
+        }
+        if (ch < 0) {
+          double x1, x2;
+          contract_pair(kp.seed, TAG_RXN, (uint32_t)c, 0, a.step, x1, x2);
+          ch = selkov_channel_fp64(kp.k, kp.tau, nF, nG, nI, x1, x2);
+        }
         if (ch > 0) {
           const uint32_t key = fk[tgt[ch]];
           if (key != 0xFFFFFFFFu) relabel_key(d, key, code[ch]);
