@@ -173,7 +173,7 @@ struct Engine : EngineBase {
   KParams<T> kp{};
   cudaStream_t st = nullptr;
   std::vector<void*> allocs;
-  int grid = 0, g_rebuild = 0, g_force = 0, g_rotate = 0;
+  int grid = 0, g_rebuild = 0, g_force = 0, g_rotate = 0, g_far = 0;
   int64_t cstep = 0;
   int time_count = 0, time_penetrate = 0;
   int64_t last_rebuild = 0;
@@ -275,12 +275,13 @@ struct Engine : EngineBase {
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     grid = nsm * 8;
     // the heavy persistent kernels run exactly one wave: SMs x resident blocks
-    int occ[3];
+    int occ[4];
     Launch<T>::occupancy(occ);
     CK(cudaGetLastError());
     g_rebuild = nsm * std::max(occ[0], 1);
     g_force = nsm * std::max(occ[1], 1);
     g_rotate = nsm * std::max(occ[2], 1);
+    g_far = nsm * std::max(occ[3], 1);
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
 
     const int64_t n = c.n_solvent, ns = 2 * (int64_t)c.n_dimers;
@@ -495,7 +496,7 @@ struct Engine : EngineBase {
     StepArgs a{};
     a.step = (uint32_t)step;
     a.grid = grid;
-    a.g_rebuild = g_rebuild; a.g_force = g_force; a.g_rotate = g_rotate;
+    a.g_rebuild = g_rebuild; a.g_force = g_force; a.g_rotate = g_rotate; a.g_far = g_far;
     a.shift[0] = shift[0]; a.shift[1] = shift[1]; a.shift[2] = shift[2];
     for (int c = 0; c < 3; ++c) a.shf[c] = (float)shift[c];
     return a;
@@ -545,7 +546,10 @@ struct Engine : EngineBase {
       a.tc_full = 0;
       a.full = 1;
     }
-    pb(PROF_REBUILD); Launch<T>::rebuild(d, kp, a, st); pe();
+    // a collision step's full pass runs split: far particles in a lean pass,
+    // the rest through the list kernel
+    if (a.full && a.mpc) { pb(PROF_REBUILD); Launch<T>::rebuild_split(d, kp, a, st); pe(); }
+    else { pb(PROF_REBUILD); Launch<T>::rebuild(d, kp, a, st); pe(); }
     pb(PROF_FINALIZE); Launch<T>::finalize_rebuild(d, kp, a, cfg.skin, st); pe();
     // a collision step's shell is used once before it is sorted into free-flight
     // and active members; other rebuilds order theirs for the coming steps

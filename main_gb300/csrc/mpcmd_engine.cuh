@@ -39,7 +39,7 @@ struct Counters {
   unsigned long long vpost;       // bits of max v^2 of the outside particles after the last collision
   unsigned long long vfar;        // bits of max v^2 of the particles off the watch list
   unsigned int n_watch;           // entries of the watch list
-  unsigned int watch_pad;
+  unsigned int n_near;            // particles the far pass of a collision rebuild deferred
   // work totals for the measurement (cleared by mpcmd_profile(ctx, 1))
   unsigned long long acc_force;   // shell entries over all k_force launches
   unsigned long long acc_rebuild; // particles visited over all k_rebuild launches
@@ -138,8 +138,10 @@ struct StepArgs {
   int g_rebuild;       // SMs x resident blocks of k_rebuild, k_force, k_rotate_main
   int g_force;
   int g_rotate;
+  int g_far;           // SMs x resident blocks of k_rebuild_far
   int watch_build;     // > 0 (the period in steps): rotate_main / rotate_shell build the watch list
   int use_watch;       // a rebuild between full passes visits the watch list only
+  int near;            // the rebuild visits the particles the far pass deferred (list in `watch`)
   int horizon;         // > 0: steps to the next collision rebuild; shell members that
                        // cannot reach an LJ cutoff or a wall before it fly freely
   double shift[3];     // collision grid shift of this step
@@ -159,6 +161,10 @@ struct Launch {
   // stored tc_defer steps ago, can be near now (for the rebuild fast path)
   static void build_bins(const Dev<T>& d, const KParams<T>& kp, int tc_defer, cudaStream_t st);
   static void rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  // collision-step full pass split in two: a lean pass over the particles
+  // whose (streamed) bin lists no sphere, which defers the others (and the
+  // shell-buffer states) to a list; then k_rebuild over that list
+  static void rebuild_split(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
   static void finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, double skin, cudaStream_t st);
   static void force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
   // kick + free flight of the shell; with a.horizon > 0 it also moves the

@@ -60,6 +60,34 @@ __device__ __forceinline__ void watch_append(unsigned int* counter, uint32_t* li
   list[base + g.thread_rank()] = i;
 }
 
+// Per-warp staging of list appends in shared memory.  All lanes of a
+// converged warp call wl_add once per iteration; the lanes with `pred` set
+// are added to the warp's buffer, which goes to the global list with one
+// atomic when it is nearly full and at the end (wl_flush).  One atomic per
+// WL_CAP entries instead of one per warp iteration keeps a list with
+// millions of appends off a single contended counter.
+constexpr int WL_CAP = 512;
+
+__device__ __forceinline__ void wl_flush(uint32_t* buf, unsigned& n, unsigned int* gcount, uint32_t* glist) {
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (lane == 0 && n) base = atomicAdd(gcount, n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (unsigned j = lane; j < n; j += 32) glist[base + j] = buf[j];
+  __syncwarp();
+  n = 0;
+}
+
+__device__ __forceinline__ void wl_add(uint32_t* buf, unsigned& n, bool pred, uint32_t v, unsigned int* gcount,
+                                       uint32_t* glist) {
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  const int lane = threadIdx.x & 31;
+  if (pred) buf[n + __popc(m & ((1u << lane) - 1u))] = v;
+  n += __popc(m);
+  __syncwarp();
+  if (n > (unsigned)(WL_CAP - 32)) wl_flush(buf, n, gcount, glist);
+}
+
 // Block maximum of a non-negative value, folded into the double bits at
 // target.  The reduction runs in T; only the block's result is widened (FP64
 // instructions are slow on this part).
@@ -517,12 +545,15 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   // A rebuild between full passes with a valid watch list visits only the
   // particles on it: no other particle can enter a list or hit a wall before
   // the next collision, and their largest speed is kept in vfar.
-  const int64_t nloop = a.use_watch ? (int64_t)d.ctr->n_watch : kp.n;
+  // The second half of a split collision pass (a.near) visits the particles
+  // the far pass deferred, listed in the same buffer.
+  const bool listed = a.use_watch || a.near;
+  const int64_t nloop = a.near ? (int64_t)d.ctr->n_near : (a.use_watch ? (int64_t)d.ctr->n_watch : kp.n);
   // sphere speed bound of the free-flight test, read once (FP64 arithmetic
   // is slow on this part)
   const T vs_bound = (a.horizon > 0 && !a.mpc) ? sphere_speed_bound<T>(d.ctr) : (T)0;
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_rebuild, (unsigned long long)nloop);
-  auto pidx = [&](int64_t k) -> int64_t { return a.use_watch ? (int64_t)d.watch[k] : k; };
+  auto pidx = [&](int64_t k) -> int64_t { return listed ? (int64_t)d.watch[k] : k; };
   const int64_t first = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31) + lane;
   uint8_t pf_f = 0;
   uint32_t pf_cell = 0;
@@ -701,9 +732,122 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
       const unsigned dmask = __ballot_sync(0xffffffffu, dist);
       unsigned peers = 0u;
       if (dist) peers = __match_any_sync(dmask, (cid << 2) | (uint32_t)sp);
+      // a listed pass holds its particles in list order, not index order:
+      // the group's smallest index is reduced over its lanes
+      uint32_t first_i = (uint32_t)i;
+      if (dist && listed) first_i = __reduce_min_sync(peers, (uint32_t)i);
       if (dist && lane == __ffs(peers) - 1) {
         // the count returned by this atomic is checked one iteration later,
         // so that the warp does not wait for it
+        if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
+          atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
+        pend_cnt = __popc(peers);
+        pend_shift = 8 * sp;
+        pend_old = atomicAdd(&d.dcnt[cid], pend_cnt << pend_shift);
+        atomicMin(&d.dfirst[4 * (size_t)cid + sp], dist_key(0, first_i));
+      }
+    }
+  }
+  if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
+    atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
+  if (a.use_watch && blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&d.ctr->maxv2, d.ctr->vfar);
+  block_max_to<T>(&d.ctr->maxv2, vmax2);
+}
+
+// First half of a split collision-step full pass (evolve_mod.f95:465-564 with
+// the collision and distribute accumulation, as k_rebuild with a.full and
+// a.mpc).  It handles the particles that need no list work: an outside state
+// whose lazily streamed position is beyond the list radius of every sphere of
+// its coarse bin enters no shell list, so it is streamed, written, and
+// accumulated here with no shell placement or shell-buffer state in the
+// kernel.  Every other particle (a state in the shell buffer, or within a
+// list radius) is left untouched and appended to the near list (d.watch,
+// n_near, staged per warp in shared memory), which k_rebuild then processes
+// in full.
+template <typename T>
+__global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp, StepArgs a) {
+  if (d.ctr->abort_step) return;
+  const T sx = step_shift<T>(a, 0), sy = step_shift<T>(a, 1), sz = step_shift<T>(a, 2);
+  T vmax2 = (T)0;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned int pend_old = 0, pend_shift = 0, pend_cnt = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_rebuild, (unsigned long long)kp.n);
+  const bool distrib = kp.kinetics != 0;
+  __shared__ uint32_t wl_buf[(TPB / 32) * WL_CAP];
+  uint32_t* wbuf = wl_buf + (threadIdx.x >> 5) * WL_CAP;
+  unsigned wn = 0;
+  const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint8_t pf_f = FLAG_HOME_SHELL;
+  uint32_t pf_cell = 0;
+  T pf_ox = 0, pf_oy = 0, pf_oz = 0, pf_vx = 0, pf_vy = 0, pf_vz = 0;
+  if (first < kp.n) {
+    pf_f = d.p.flag[first]; pf_cell = d.p.cell[first];
+    pf_ox = d.p.ox[first]; pf_oy = d.p.oy[first]; pf_oz = d.p.oz[first];
+    pf_vx = d.p.vx[first]; pf_vy = d.p.vy[first]; pf_vz = d.p.vz[first];
+  }
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < kp.n; base += stride) {
+    const int64_t i = base + lane;
+    const bool in = i < kp.n;
+    const uint8_t f = pf_f;
+    uint32_t cell = pf_cell;
+    T ox = pf_ox, oy = pf_oy, oz = pf_oz;
+    T vx = pf_vx, vy = pf_vy, vz = pf_vz;
+    const int64_t inext = i + stride;
+    if (inext < kp.n) {
+      pf_f = d.p.flag[inext]; pf_cell = d.p.cell[inext];
+      pf_ox = d.p.ox[inext]; pf_oy = d.p.oy[inext]; pf_oz = d.p.oz[inext];
+      pf_vx = d.p.vx[inext]; pf_vy = d.p.vy[inext]; pf_vz = d.p.vz[inext];
+    }
+    bool far = in && !(f & FLAG_HOME_SHELL);
+    bool near = in && !far;
+    uint8_t sp = f & FLAG_SPECIES;
+    uint32_t cid = 0;
+    if (far) {
+      const uint32_t cell0 = cell;
+      const T vx0 = vx, vy0 = vy, vz0 = vz;
+      int lag = 0;
+      if (!(f & FLAG_INLIST)) lag = (f & (FLAG_FRESH | FLAG_PASSIVE)) ? a.tc : a.tc_full;
+      if (lag > 0) {
+        uint8_t ff = sp;
+        stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, ff, true, lag);
+        sp = ff & FLAG_SPECIES;
+      }
+      // within the list radius of a sphere of its bin: the whole particle
+      // goes to k_rebuild (lists, shell placement)
+      if (kp.ns > 0) {
+        const int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
+        unsigned int nc = d.bin_cnt[bin];
+        nc = nc < (unsigned)BIN_SLOTS ? nc : (unsigned)BIN_SLOTS;
+        const uint16_t* bl = d.bin_list + (size_t)bin * BIN_SLOTS;
+        for (unsigned int q = 0; q < nc && !near; ++q) {
+          const int sph = bl[q];
+          T dx, dy, dz;
+          if (sep2(kp, cell, ox, oy, oz, d.srel[sph], dx, dy, dz) <= kp.full2[sph & 1]) near = true;
+        }
+        far = !near;
+      }
+      if (far) {
+        const T v2 = vx * vx + vy * vy + vz * vz;
+        vmax2 = v2 > vmax2 ? v2 : vmax2;
+        if (cell != cell0) d.p.cell[i] = cell;
+        if (lag > 0) { d.p.ox[i] = ox; d.p.oy[i] = oy; d.p.oz[i] = oz; }
+        if (vx != vx0 || vy != vy0 || vz != vz0) { d.p.vx[i] = vx; d.p.vy[i] = vy; d.p.vz[i] = vz; }
+        if (sp != f) d.p.flag[i] = sp;
+        const uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
+        d.skey[i] = key;
+        accum_coll<T>(d.acc, key, vx, vy, vz);
+        cid = unshifted_id(kp.lx, kp.ly, cell);
+      }
+    }
+    wl_add(wbuf, wn, near, (uint32_t)i, &d.ctr->n_near, d.watch);
+    // distribute_mod.f95:95-182 counts and first members as in k_rebuild
+    if (distrib) {
+      const bool dist = far;
+      const unsigned dmask = __ballot_sync(0xffffffffu, dist);
+      unsigned peers = 0u;
+      if (dist) peers = __match_any_sync(dmask, (cid << 2) | (uint32_t)sp);
+      if (dist && lane == __ffs(peers) - 1) {
         if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
           atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
         pend_cnt = __popc(peers);
@@ -713,10 +857,21 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
       }
     }
   }
+  wl_flush(wbuf, wn, &d.ctr->n_near, d.watch);
   if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
     atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
-  if (a.use_watch && blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&d.ctr->maxv2, d.ctr->vfar);
   block_max_to<T>(&d.ctr->maxv2, vmax2);
+}
+
+template <typename T>
+void Launch<T>::rebuild_split(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
+  cudaMemsetAsync(&d.ctr->n_near, 0, sizeof(unsigned int), st);
+  k_rebuild_far<T><<<a.g_far, TPB, 0, st>>>(d, kp, a);
+  StepArgs b = a;
+  b.near = 1;
+  b.use_watch = 0;
+  k_rebuild<T><<<a.g_rebuild, TPB, 0, st>>>(d, kp, b);
+  LAUNCH_COUNT(); LAUNCH_COUNT();
 }
 
 template <typename T>
@@ -1909,10 +2064,11 @@ void Launch<T>::rotate_main(const Dev<T>& d, const KParams<T>& kp, const StepArg
 
 template <typename T>
 void Launch<T>::occupancy(int* blocks) {
-  blocks[0] = blocks[1] = blocks[2] = 0;
+  blocks[0] = blocks[1] = blocks[2] = blocks[3] = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], k_rebuild<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], k_force<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], k_rotate_main<T>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], k_rebuild_far<T>, TPB, 0);
 }
 
 // ---------------------------------------------------- shell home moves ----
