@@ -2000,14 +2000,23 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
   // vfar2 is the largest v^2 of the others (constant until that collision)
   T vfar2 = (T)0;
   const T vs = sphere_speed_bound<T>(d.ctr);
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < kp.n; i0 += 2 * stride) {
+  // watch-list appends staged per warp (the loop is warp-uniform)
+  __shared__ uint32_t wl_buf[(TPB / 32) * WL_CAP];
+  uint32_t* wbuf = wl_buf + (threadIdx.x >> 5) * WL_CAP;
+  unsigned wn = 0;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < kp.n; base += 2 * stride) {
+    const int64_t i0 = base + lane;
     const int64_t i1 = i0 + stride;
+    const bool h0 = i0 < kp.n;
     const bool h1 = i1 < kp.n;
-    const uint8_t f0 = d.p.flag[i0];
+    bool w0 = false, w1 = false;
+    const uint8_t f0 = h0 ? d.p.flag[i0] : FLAG_HOME_SHELL;
     const uint8_t f1 = h1 ? d.p.flag[i1] : FLAG_HOME_SHELL;
-    const uint32_t k0 = d.skey[i0];
+    const uint32_t k0 = h0 ? d.skey[i0] : 0u;
     const uint32_t k1 = h1 ? d.skey[i1] : 0u;
-    T vx0 = d.p.vx[i0], vy0 = d.p.vy[i0], vz0 = d.p.vz[i0];
+    T vx0 = (T)0, vy0 = (T)0, vz0 = (T)0;
+    if (h0) { vx0 = d.p.vx[i0]; vy0 = d.p.vy[i0]; vz0 = d.p.vz[i0]; }
     T vx1 = (T)0, vy1 = (T)0, vz1 = (T)0;
     if (h1) { vx1 = d.p.vx[i1]; vy1 = d.p.vy[i1]; vz1 = d.p.vz[i1]; }
     const bool r0 = !(f0 & FLAG_HOME_SHELL), r1 = !(f1 & FLAG_HOME_SHELL);
@@ -2034,8 +2043,8 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
       const T w = vx0 * vx0 + vy0 * vy0 + vz0 * vz0;
       vmax2 = w > vmax2 ? w : vmax2;
       if (a.watch_build) {
-        if (watch_test(kp, g0, c0, vz0, w, a.watch_build, vs)) watch_append(&d.ctr->n_watch, d.watch, (uint32_t)i0);
-        else vfar2 = w > vfar2 ? w : vfar2;
+        w0 = watch_test(kp, g0, c0, vz0, w, a.watch_build, vs);
+        if (!w0) vfar2 = w > vfar2 ? w : vfar2;
       }
     }
     if (r1) {
@@ -2044,11 +2053,16 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
       const T w = vx1 * vx1 + vy1 * vy1 + vz1 * vz1;
       vmax2 = w > vmax2 ? w : vmax2;
       if (a.watch_build) {
-        if (watch_test(kp, g1, c1, vz1, w, a.watch_build, vs)) watch_append(&d.ctr->n_watch, d.watch, (uint32_t)i1);
-        else vfar2 = w > vfar2 ? w : vfar2;
+        w1 = watch_test(kp, g1, c1, vz1, w, a.watch_build, vs);
+        if (!w1) vfar2 = w > vfar2 ? w : vfar2;
       }
     }
+    if (a.watch_build) {
+      wl_add(wbuf, wn, w0, (uint32_t)i0, &d.ctr->n_watch, d.watch);
+      wl_add(wbuf, wn, w1, (uint32_t)i1, &d.ctr->n_watch, d.watch);
+    }
   }
+  if (a.watch_build) wl_flush(wbuf, wn, &d.ctr->n_watch, d.watch);
   block_max_to<T>(&d.ctr->vpost, vmax2);
   if (a.watch_build) {
     __syncthreads();   // block_max_to's shared buffer is reused
