@@ -363,7 +363,7 @@ struct Engine : EngineBase {
     int64_t nbins = (int64_t)kp.nbx * kp.nby * kp.nbz;
     r |= alloc(d.bin_cnt, nbins); r |= alloc(d.bin_list, nbins * BIN_SLOTS);
     r |= alloc(d.gapf, nbins); r |= alloc(d.watch, n);
-    r |= alloc(d.sph_cnt, ns1); r |= alloc(d.sph_base, ns1);
+    r |= alloc(d.sph_cnt, ns1 * SHELL_CLASSES); r |= alloc(d.sph_base, ns1 * SHELL_CLASSES);
     if (sizeof(T) == 4) { float4* a = nullptr; r |= alloc(a, kp.ncell_shift); d.acc = a; }
     else { double* a = nullptr; r |= alloc(a, 4 * kp.ncell_shift); d.acc = a; }
     r |= alloc(d.rot, 6 * kp.ncell_shift);

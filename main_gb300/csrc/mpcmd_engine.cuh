@@ -7,7 +7,8 @@
 
 namespace mpcmd {
 
-constexpr int TPB = 256;   // threads per block of the grid-stride kernels
+constexpr int TPB = 256;
+constexpr int SHELL_CLASSES = 3;   // pair classes of the shell ordering (k_shell_hist)   // threads per block of the grid-stride kernels
 
 // Error bits accumulated on the device (mapped to mpcmd_status on the host).
 enum : int {
@@ -112,8 +113,8 @@ struct Dev {
   uint32_t* order_rank;    // [ncell] position of each cell in the sort order
   uint32_t* watch;         // [n] particles that can come near a sphere or a wall before the next collision
   uint32_t* gapf;          // [nbins] bits of a lower bound on (distance to a sphere - list radius), >= 0
-  uint32_t* sph_cnt;       // [ns] shell entries per first sphere (shell ordering)
-  uint32_t* sph_base;      // [ns] first slot of each sphere's entries
+  uint32_t* sph_cnt;       // [ns * 3] shell entries per (first sphere, pair class) (shell ordering)
+  uint32_t* sph_base;      // [ns * 3] first slot of each bucket's entries
   uint32_t* scnt;          // [ncell] sort scratch
   uint32_t* sstart;        // [ncell]
   uint32_t* sfill;         // [ncell]

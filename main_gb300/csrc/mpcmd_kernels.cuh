@@ -1213,11 +1213,19 @@ void Launch<T>::rotate_shell(const Dev<T>& d, const KParams<T>& kp, const StepAr
 }
 
 // ------------------------------------------------------- shell ordering ----
-// Counting sort of the shell entries by their first sphere: the entries a warp
-// processes then mostly share their spheres, so the per-sphere warp
-// reductions of k_force run once or twice per warp instead of once per sphere
-// present.  The order within a sphere is not specified (results do not depend
-// on it beyond the summation order of the FP64 sphere-force atomics).
+// Counting sort of the shell entries by (first sphere, pair class): the
+// entries a warp processes then mostly share their spheres and their pair
+// count, so the per-sphere warp reductions of k_force run once or twice per
+// warp instead of once per sphere present, and a warp of single-pair entries
+// does not loop over second pairs.  Classes: 0 one pair, 1 the second pair is
+// the first sphere's dimer partner, 2 any other second pair.  The order
+// within a bucket is not specified (results do not depend on it beyond the
+// summation order of the FP64 sphere-force atomics).
+__device__ __forceinline__ int shell_bucket(uint32_t s01, int np) {
+  const int s0 = (int)(s01 & 0xFFFFu), s1 = (int)(s01 >> 16);
+  const int cls = np <= 1 ? 0 : (s1 == (s0 ^ 1) ? 1 : 2);
+  return s0 * SHELL_CLASSES + cls;
+}
 template <typename T>
 __global__ void k_shell_hist(Dev<T> d, KParams<T> kp) {
   if (d.ctr->abort_step) return;
@@ -1228,10 +1236,11 @@ __global__ void k_shell_hist(Dev<T> d, KParams<T> kp) {
     const int64_t j = base + lane;
     int s = -1;
     if (j < (int64_t)nin) {
-      s = d.sh2.sph[(size_t)j * PAIRMAX];
-      if (!chk(s < kp.ns, d.ctr, 123, s)) s = -1;
+      const uint32_t s01 = *reinterpret_cast<const uint32_t*>(d.sh2.sph + (size_t)j * PAIRMAX);
+      s = (int)(s01 & 0xFFFFu) < kp.ns ? shell_bucket(s01, d.sh2.np[j]) : -1;
+      if (!chk(s >= 0, d.ctr, 123, s01)) s = -1;
     }
-    // one atomic per sphere present in the warp
+    // one atomic per bucket present in the warp
     const unsigned peers = __match_any_sync(0xffffffffu, s);
     if (s >= 0 && lane == __ffs(peers) - 1) atomicAdd(&d.sph_cnt[s], (unsigned)__popc(peers));
   }
@@ -1242,8 +1251,9 @@ __global__ void k_shell_scan(Dev<T> d, KParams<T> kp) {
   if (d.ctr->abort_step) return;
   // one block: exclusive scan of the ns counts, which become the cursors
   __shared__ uint32_t part[TPB];
-  const int per = (kp.ns + TPB - 1) / TPB;
-  const int lo = threadIdx.x * per, hi = min(lo + per, kp.ns);
+  const int nbk = kp.ns * SHELL_CLASSES;
+  const int per = (nbk + TPB - 1) / TPB;
+  const int lo = threadIdx.x * per, hi = min(lo + per, nbk);
   uint32_t sum = 0;
   for (int s = lo; s < hi; ++s) sum += d.sph_cnt[s];
   part[threadIdx.x] = sum;
@@ -1269,10 +1279,10 @@ __global__ void k_shell_scatter(Dev<T> d, KParams<T> kp) {
     int s = -1;
     if (j < (int64_t)nin) {
       packed = *reinterpret_cast<const uint4*>(d.sh2.sph + (size_t)j * PAIRMAX);
-      s = (int)(packed.x & 0xFFFFu);
-      if (!chk(s < kp.ns, d.ctr, 124, s)) s = -1;
+      s = (int)(packed.x & 0xFFFFu) < kp.ns ? shell_bucket(packed.x, d.sh2.np[j]) : -1;
+      if (!chk(s >= 0, d.ctr, 124, packed.x)) s = -1;
     }
-    // one atomic per sphere present in the warp; its lanes take consecutive slots
+    // one atomic per bucket present in the warp; its lanes take consecutive slots
     const unsigned peers = __match_any_sync(0xffffffffu, s);
     const int lead = __ffs(peers) - 1;
     uint32_t first = 0;
@@ -1297,13 +1307,14 @@ __global__ void k_shell_scatter(Dev<T> d, KParams<T> kp) {
 
 template <typename T>
 __global__ void k_shell_clear_counts(Dev<T> d, KParams<T> kp) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < kp.ns; s += gridDim.x * blockDim.x) d.sph_cnt[s] = 0u;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < kp.ns * SHELL_CLASSES; s += gridDim.x * blockDim.x)
+    d.sph_cnt[s] = 0u;
 }
 
 template <typename T>
 void Launch<T>::sort_shell(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
   if (kp.ns == 0) return;
-  k_shell_clear_counts<T><<<(kp.ns + TPB - 1) / TPB, TPB, 0, st>>>(d, kp);
+  k_shell_clear_counts<T><<<(kp.ns * SHELL_CLASSES + TPB - 1) / TPB, TPB, 0, st>>>(d, kp);
   k_shell_hist<T><<<1024, TPB, 0, st>>>(d, kp);
   k_shell_scan<T><<<1, TPB, 0, st>>>(d, kp);
   k_shell_scatter<T><<<1024, TPB, 0, st>>>(d, kp);
