@@ -770,30 +770,41 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
   const T sx = step_shift<T>(a, 0), sy = step_shift<T>(a, 1), sz = step_shift<T>(a, 2);
   T vmax2 = (T)0;
   const int lane = threadIdx.x & 31;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   unsigned int pend_old = 0, pend_shift = 0, pend_cnt = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_rebuild, (unsigned long long)kp.n);
   const bool distrib = kp.kinetics != 0;
   __shared__ uint32_t wl_buf[(TPB / 32) * WL_CAP];
   uint32_t* wbuf = wl_buf + (threadIdx.x >> 5) * WL_CAP;
   unsigned wn = 0;
-  const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // Blocks take tiles of FAR_TILE consecutive particles in a grid stride,
+  // the warps of a block interleaved in 32-particle steps inside a tile: the
+  // GPU still sweeps the arrays front to back, and the near list a warp
+  // stages holds particles of one tile at a time, so the shell built from it
+  // keeps their spatial (cell) order.
+  constexpr int FAR_STEPS = 16;
+  constexpr int64_t FAR_TILE = (int64_t)FAR_STEPS * TPB;
+  const int64_t tile_stride = (int64_t)gridDim.x * FAR_TILE;
+  int64_t i = (int64_t)blockIdx.x * FAR_TILE + threadIdx.x;
+  int step = 0;
+  auto advance = [&](int64_t j, int st) -> int64_t {   // the index after j (at step st of its tile)
+    return st + 1 < FAR_STEPS ? j + TPB : j - (int64_t)(FAR_STEPS - 1) * TPB + tile_stride;
+  };
   uint8_t pf_f = FLAG_HOME_SHELL;
   uint32_t pf_cell = 0;
   T pf_ox = 0, pf_oy = 0, pf_oz = 0, pf_vx = 0, pf_vy = 0, pf_vz = 0;
-  if (first < kp.n) {
-    pf_f = d.p.flag[first]; pf_cell = d.p.cell[first];
-    pf_ox = d.p.ox[first]; pf_oy = d.p.oy[first]; pf_oz = d.p.oz[first];
-    pf_vx = d.p.vx[first]; pf_vy = d.p.vy[first]; pf_vz = d.p.vz[first];
+  if (i < kp.n) {
+    pf_f = d.p.flag[i]; pf_cell = d.p.cell[i];
+    pf_ox = d.p.ox[i]; pf_oy = d.p.oy[i]; pf_oz = d.p.oz[i];
+    pf_vx = d.p.vx[i]; pf_vy = d.p.vy[i]; pf_vz = d.p.vz[i];
   }
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < kp.n; base += stride) {
-    const int64_t i = base + lane;
+  // the loop runs while the warp's step base is inside the array (warp-uniform)
+  for (; i - lane < kp.n; i = advance(i, step), step = step + 1 < FAR_STEPS ? step + 1 : 0) {
     const bool in = i < kp.n;
     const uint8_t f = pf_f;
     uint32_t cell = pf_cell;
     T ox = pf_ox, oy = pf_oy, oz = pf_oz;
     T vx = pf_vx, vy = pf_vy, vz = pf_vz;
-    const int64_t inext = i + stride;
+    const int64_t inext = advance(i, step);
     if (inext < kp.n) {
       pf_f = d.p.flag[inext]; pf_cell = d.p.cell[inext];
       pf_ox = d.p.ox[inext]; pf_oy = d.p.oy[inext]; pf_oz = d.p.oz[inext];
