@@ -2015,7 +2015,6 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
   if (d.ctr->abort_step) return;
   // two particles per thread and iteration: all loads and both table gathers
   // are issued before the first store
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   T vmax2 = (T)0;   // speed bound of the outside particles until the next collision
   // with a.watch_build (= the period in steps): the particles that can come
   // near a sphere or a wall before the next collision join the watch list;
@@ -2027,9 +2026,17 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
   uint32_t* wbuf = wl_buf + (threadIdx.x >> 5) * WL_CAP;
   unsigned wn = 0;
   const int lane = threadIdx.x & 31;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < kp.n; base += 2 * stride) {
-    const int64_t i0 = base + lane;
-    const int64_t i1 = i0 + stride;
+  // blocks take tiles of ROT_TILE consecutive particles in a grid stride (two
+  // 256-particle steps per iteration), so that the watch list a warp stages
+  // keeps the particles' cell order
+  constexpr int ROT_STEPS = 16;
+  constexpr int64_t ROT_TILE = (int64_t)ROT_STEPS * TPB;
+  const int64_t tile_stride = (int64_t)gridDim.x * ROT_TILE;
+  int step = 0;
+  for (int64_t i0 = (int64_t)blockIdx.x * ROT_TILE + threadIdx.x; i0 - lane < kp.n;
+       i0 = step + 2 < ROT_STEPS ? i0 + 2 * TPB : i0 - (int64_t)(ROT_STEPS - 2) * TPB + tile_stride,
+       step = step + 2 < ROT_STEPS ? step + 2 : 0) {
+    const int64_t i1 = i0 + TPB;
     const bool h0 = i0 < kp.n;
     const bool h1 = i1 < kp.n;
     bool w0 = false, w1 = false;
