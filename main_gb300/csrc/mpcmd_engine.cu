@@ -362,6 +362,7 @@ struct Engine : EngineBase {
     r |= alloc(d.srel, ns1); r |= alloc(d.facc, 4 * ns1); r |= alloc(d.fmot, 4 * ns1); r |= alloc(d.dpot, nd1);
     int64_t nbins = (int64_t)kp.nbx * kp.nby * kp.nbz;
     r |= alloc(d.bin_cnt, nbins); r |= alloc(d.bin_list, nbins * BIN_SLOTS);
+    r |= alloc(d.bin_mask, (nbins + 31) / 32);
     r |= alloc(d.gapf, nbins); r |= alloc(d.watch, n);
     r |= alloc(d.sph_cnt, ns1 * SHELL_CLASSES); r |= alloc(d.sph_base, ns1 * SHELL_CLASSES);
     if (sizeof(T) == 4) { float4* a = nullptr; r |= alloc(a, kp.ncell_shift); d.acc = a; }

@@ -103,6 +103,7 @@ struct Dev {
   double* fmot;            // [ns*4] motor-motor force and potential (j < k part)
   double* dpot;            // [nd] potential of each dimer at the last force evaluation
   uint32_t* bin_cnt;       // [nbins]
+  uint32_t* bin_mask;      // [ceil(nbins / 32)] bit b set: bin b lists a sphere
   uint16_t* bin_list;      // [nbins * BIN_SLOTS]
   void* acc;               // [ncell_shift] float4 (FP32) or double4 (FP64): n, sum v
   T* rot;                  // [ncell_shift * 6] centre-of-mass velocity and axis

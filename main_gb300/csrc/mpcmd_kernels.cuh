@@ -66,7 +66,7 @@ __device__ __forceinline__ void watch_append(unsigned int* counter, uint32_t* li
 // atomic when it is nearly full and at the end (wl_flush).  One atomic per
 // WL_CAP entries instead of one per warp iteration keeps a list with
 // millions of appends off a single contended counter.
-constexpr int WL_CAP = 512;
+constexpr int WL_CAP = 448;
 
 __device__ __forceinline__ void wl_flush(uint32_t* buf, unsigned& n, unsigned int* gcount, uint32_t* glist) {
   const int lane = threadIdx.x & 31;
@@ -462,26 +462,35 @@ __global__ void k_bins_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn, int t
   }
 }
 
+// Sorts each bin's list and writes the bitmask of the bins that list a sphere
+// (one word per 32 consecutive bins, from the warp's ballot).
 template <typename T>
 __global__ void k_bins_sort(Dev<T> d, int nbins) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbins) return;
-  unsigned int n = min(d.bin_cnt[b], (unsigned)BIN_SLOTS);
-  uint16_t* l = d.bin_list + (size_t)b * BIN_SLOTS;
-  for (unsigned int i = 1; i < n; ++i) {
-    uint16_t v = l[i];
-    int j = (int)i - 1;
-    while (j >= 0 && l[j] > v) { l[j + 1] = l[j]; --j; }
-    l[j + 1] = v;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned int n = 0u;
+  if (b < nbins) {
+    n = min(d.bin_cnt[b], (unsigned)BIN_SLOTS);
+    uint16_t* l = d.bin_list + (size_t)b * BIN_SLOTS;
+    for (unsigned int i = 1; i < n; ++i) {
+      uint16_t v = l[i];
+      int j = (int)i - 1;
+      while (j >= 0 && l[j] > v) { l[j + 1] = l[j]; --j; }
+      l[j + 1] = v;
+    }
+    if (n < d.bin_cnt[b]) d.bin_cnt[b] = n;
   }
-  if (n < d.bin_cnt[b]) d.bin_cnt[b] = n;
+  const unsigned m = __ballot_sync(0xffffffffu, n > 0u);
+  if ((threadIdx.x & 31) == 0 && b < nbins) d.bin_mask[b >> 5] = m;
 }
 
 template <typename T>
 void Launch<T>::build_bins(const Dev<T>& d, const KParams<T>& kp, int tc_defer, cudaStream_t st) {
   int nbins = kp.nbx * kp.nby * kp.nbz;
   cudaMemsetAsync(d.bin_cnt, 0, sizeof(uint32_t) * nbins, st);
-  if (kp.ns == 0) return;
+  if (kp.ns == 0) {
+    cudaMemsetAsync(d.bin_mask, 0, sizeof(uint32_t) * ((nbins + 31) / 32), st);
+    return;
+  }
   double Rc = sqrt((double)kp.full2[0]) + 1e-6, Rn = sqrt((double)kp.full2[1]) + 1e-6;
   k_bins_fill<T><<<kp.ns, 128, 0, st>>>(d, kp, Rc, Rn, tc_defer);
   k_bins_sort<T><<<(nbins + 255) / 256, 256, 0, st>>>(d, nbins);
@@ -491,6 +500,9 @@ void Launch<T>::build_bins(const Dev<T>& d, const KParams<T>& kp, int tc_defer, 
 __device__ __forceinline__ int bin_of(int lx, int ly, int nbx, int nby, uint32_t cell) {
   return cell_x(cell) / BIN_EDGE + nbx * (cell_y(cell) / BIN_EDGE + nby * (cell_z(cell) / BIN_EDGE));
 }
+
+// Bins whose bitmask fits in shared memory (32 KB: a 256^3-cell box).
+constexpr int BIN_MASK_SMEM_WORDS = 8192;
 
 // Free-flight test of a shell member.  The reference integrates every member
 // of its inside list each MD step (evolve_mod.f95:225-316).  A member that,
@@ -773,6 +785,15 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
   unsigned int pend_old = 0, pend_shift = 0, pend_cnt = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.ctr->acc_rebuild, (unsigned long long)kp.n);
   const bool distrib = kp.kinetics != 0;
+  // the bitmask of the bins that list a sphere, in shared memory when it fits:
+  // most particles are far from every sphere and skip the bin-count load
+  __shared__ uint32_t smask[BIN_MASK_SMEM_WORDS];
+  const int nmask = (kp.nbx * kp.nby * kp.nbz + 31) / 32;
+  const bool use_smask = kp.ns > 0 && nmask <= BIN_MASK_SMEM_WORDS;
+  if (use_smask) {
+    for (int w = threadIdx.x; w < nmask; w += blockDim.x) smask[w] = d.bin_mask[w];
+    __syncthreads();
+  }
   __shared__ uint32_t wl_buf[(TPB / 32) * WL_CAP];
   uint32_t* wbuf = wl_buf + (threadIdx.x >> 5) * WL_CAP;
   unsigned wn = 0;
@@ -826,8 +847,8 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
       }
       // within the list radius of a sphere of its bin: the whole particle
       // goes to k_rebuild (lists, shell placement)
-      if (kp.ns > 0) {
-        const int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
+      const int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
+      if (kp.ns > 0 && (!use_smask || ((smask[bin >> 5] >> (bin & 31)) & 1u))) {
         unsigned int nc = d.bin_cnt[bin];
         nc = nc < (unsigned)BIN_SLOTS ? nc : (unsigned)BIN_SLOTS;
         const uint16_t* bl = d.bin_list + (size_t)bin * BIN_SLOTS;
