@@ -6,8 +6,8 @@ sphere dimers plus one reactive multiparticle collision (main_pattern.f95:
 203-225 iterated 50 times).  Particle-steps = solvent particles x MD steps, all
 50 MD steps counted for every particle.  The default workload is the 256^3-cell
 Selkov-kinetics run (167,772,160 solvent particles, 512 dimers), synthetic and
-seeded; its state (about 5 GB) is larger than L2, so no flush is needed between
-timed steps.
+seeded; its resident state (24 GB) is far larger than L2, so no flush is needed
+between timed steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2] [--scale 1.0]
     python bench.py --impl reference ...   (times the FP64 CPU restatement)
