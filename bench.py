@@ -269,7 +269,7 @@ def gpu_arm(args, ws, rk, lr, dist):
         for _ in range(args.steps):
             e.run(S)
             e.observables()
-        out = e.download_state()
+        e.download_state(out=host)   # into the same page-locked buffers
         t1 = time.perf_counter()
         state_bytes = N * (6 * 8 + 4) + ns * 3 * 8 * 3
         obs_bytes = 8 * 16 + ns * 3 * 8 + cfg["n_dimers"] * 8

@@ -173,11 +173,26 @@ class Engine:
                                          _ptr(dpos, C.c_double), _ptr(dvel, C.c_double), _ptr(dfrc, C.c_double)),
                 "upload_state")
 
-    def download_state(self):
+    def download_state(self, out=None):
+        """The host state in the reference layout.  `out`: arrays to fill (for
+        example page-locked ones, which the copies reach at full link speed):
+        x..vz float64 [n], flag int32 [n], dpos/dvel/dforce float64 [n_spheres, 3],
+        all C-contiguous; new arrays are allocated when it is None."""
         n, ns = self.n, max(self.ns, 1)
-        out = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
-        out["flag"] = np.zeros(n, dtype=np.int32)
-        out["dpos"] = np.zeros((ns, 3)); out["dvel"] = np.zeros((ns, 3)); out["dforce"] = np.zeros((ns, 3))
+        if out is None:
+            out = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
+            out["flag"] = np.zeros(n, dtype=np.int32)
+            out["dpos"] = np.zeros((ns, 3)); out["dvel"] = np.zeros((ns, 3)); out["dforce"] = np.zeros((ns, 3))
+        else:
+            want = {k: (np.float64, (n,)) for k in ("x", "y", "z", "vx", "vy", "vz")}
+            want["flag"] = (np.int32, (n,))
+            for k in ("dpos", "dvel", "dforce"):
+                want[k] = (np.float64, (ns, 3))
+            for k, (dt, shape) in want.items():
+                a = out[k]
+                if a.dtype != dt or a.shape != shape or not a.flags["C_CONTIGUOUS"] or not a.flags["WRITEABLE"]:
+                    raise ValueError("download_state: out[%r] must be a writeable C-contiguous %s array of shape %s"
+                                     % (k, np.dtype(dt).name, shape))
         self._c(lib().mpcmd_download_state(self.h, *[_ptr(out[k], C.c_double) for k in ("x", "y", "z", "vx", "vy", "vz")],
                                            _ptr(out["flag"], C.c_int32), _ptr(out["dpos"], C.c_double),
                                            _ptr(out["dvel"], C.c_double), _ptr(out["dforce"], C.c_double)),

@@ -2250,9 +2250,47 @@ void Launch<T>::sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
 // --------------------------------------------------------------- reductions --
 template <typename T>
 __global__ void k_observables(Dev<T> d, KParams<T> kp, double m0, double m1, double m2, double m3) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  if (sizeof(T) == 4) {
+    // FP32 build: compensated (Kahan) FP32 sums per thread, widened to FP64
+    // for the reduction over threads; FP64 arithmetic per particle would run
+    // at the part's FP64 rate
+    const float mf0 = (float)m0, mf1 = (float)m1, mf2 = (float)m2, mf3 = (float)m3;
+    float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
+    uint32_t cnt[4] = {0u, 0u, 0u, 0u};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+      const uint8_t f = d.p.flag[i];
+      float vx, vy, vz;
+      int sp;
+      if (f & FLAG_HOME_SHELL) {
+        const uint32_t j = d.p.cell[i];
+        vx = (float)d.sh.vx[j]; vy = (float)d.sh.vy[j]; vz = (float)d.sh.vz[j];
+        sp = d.sh.flag[j] & FLAG_SPECIES;
+      } else {
+        vx = (float)d.p.vx[i]; vy = (float)d.p.vy[i]; vz = (float)d.p.vz[i];
+        sp = f & FLAG_SPECIES;
+      }
+      const float m = sp == 0 ? mf0 : (sp == 1 ? mf1 : (sp == 2 ? mf2 : mf3));
+      const float term[4] = {m * vx, m * vy, m * vz, 0.5f * m * (vx * vx + vy * vy + vz * vz)};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float y = term[k] - cmp[k];
+        const float t = sum[k] + y;
+        cmp[k] = (t - sum[k]) - y;
+        sum[k] = t;
+      }
+      cnt[0] += sp == 0; cnt[1] += sp == 1; cnt[2] += sp == 2; cnt[3] += sp == 3;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      double v = k < 4 ? widen_f32(sum[k]) - widen_f32(cmp[k]) : (double)cnt[k - 4];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if ((threadIdx.x & 31) == 0) atomicAdd(&d.ctr->sums[k], v);
+    }
+    return;
+  }
   const double mass[4] = {m0, m1, m2, m3};
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
     uint8_t f = d.p.flag[i];
     double vx, vy, vz;

@@ -107,3 +107,27 @@ def test_dimer_axes(case):
     np.testing.assert_allclose(vd, (vcm * d / ln[:, None]).sum(axis=1), rtol=0, atol=1e-12)
     # the bond is held at Dcn by RATTLE, so both normalisations agree closely
     assert np.abs(ln - e.cfg["dcn"]).max() < 1e-5
+
+
+@pytest.mark.parametrize("case", ["c0", "c1", "c2"])
+@pytest.mark.parametrize("prec", [64, 32])
+def test_observables_match_the_downloaded_state(case, prec):
+    """mpcmd_observables' solvent sums (output_mod.f95:681-806) against FP64
+    sums over the downloaded host state: species counts exact; momentum and
+    kinetic energy within 1e-6 of the sum of the magnitudes (the FP32 build
+    sums compensated FP32 terms per thread and reduces in FP64)."""
+    cfg = CASES[case](prec)
+    e = Engine(cfg)
+    e.initial()
+    e.prepare()
+    e.run(37)
+    st = e.download_state()
+    obs = e.observables()
+    m = np.asarray(cfg["mass"], float)[st["flag"]]
+    v = np.stack([st["vx"], st["vy"], st["vz"]])
+    p = (m * v).sum(axis=1)
+    pabs = np.abs(m * v).sum(axis=1)
+    ke = 0.5 * (m * (v * v).sum(axis=0)).sum()
+    np.testing.assert_array_equal(obs["species_count"], np.bincount(st["flag"], minlength=4))
+    assert np.all(np.abs(obs["solvent_momentum"] - p) <= 1e-6 * pabs + 1e-9), (obs["solvent_momentum"], p)
+    assert abs(obs["kinetic_solvent"] - ke) <= 1e-6 * ke
