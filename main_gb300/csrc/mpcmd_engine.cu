@@ -172,6 +172,10 @@ struct Engine : EngineBase {
   Dev<T> d{};
   KParams<T> kp{};
   cudaStream_t st = nullptr;
+  // host exchange: copies on cst overlap the conversions on st, through two
+  // staging buffers (events: copy done, conversion done, per buffer)
+  cudaStream_t cst = nullptr;
+  cudaEvent_t xev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<void*> allocs;
   int grid = 0, g_rebuild = 0, g_force = 0, g_rotate = 0, g_far = 0;
   int64_t cstep = 0;
@@ -227,7 +231,10 @@ struct Engine : EngineBase {
     for (auto& r : prof_open) { cudaEventDestroy(r.second.first); cudaEventDestroy(r.second.second); }
     for (cudaEvent_t e : prof_pool) cudaEventDestroy(e);
     for (cudaEvent_t e : marks) if (e) cudaEventDestroy(e);
+    if (cst) cudaStreamSynchronize(cst);
+    for (cudaEvent_t e : xev) if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
+    if (cst) cudaStreamDestroy(cst);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -283,6 +290,8 @@ struct Engine : EngineBase {
     g_rotate = nsm * std::max(occ[2], 1);
     g_far = nsm * std::max(occ[3], 1);
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : xev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 
     const int64_t n = c.n_solvent, ns = 2 * (int64_t)c.n_dimers;
     kp.lx = c.lx; kp.ly = c.ly; kp.lz = c.lz;
@@ -354,6 +363,7 @@ struct Engine : EngineBase {
     r |= alloc(d.skey, n);
     r |= alloc(d.sidx, n);
     r |= alloc(d.staging, n);
+    r |= alloc(d.staging2, n);
     r |= alloc(d.staging_i, n);
     r |= alloc_shell(d.sh, cap);
     r |= alloc_shell(d.sh2, cap);
@@ -454,7 +464,27 @@ struct Engine : EngineBase {
   int upload(const double* x, const double* y, const double* z, const double* vx, const double* vy,
              const double* vz, const int32_t* flag, const double* dpos, const double* dvel,
              const double* dforce) override {
-    Launch<T>::upload_convert(d, kp, x, y, z, vx, vy, vz, flag, st);
+    // component c is copied into buffer c & 1 on cst while component c - 1 is
+    // converted on st; a buffer is refilled only after its last conversion
+    const double* comps[6] = {x, y, z, vx, vy, vz};
+    double* buf[2] = {d.staging, d.staging2};
+    cudaEvent_t copied[2] = {xev[0], xev[1]}, used[2] = {xev[2], xev[3]};
+    CK(cudaEventRecord(used[0], st));
+    CK(cudaEventRecord(used[1], st));
+    CK(cudaStreamWaitEvent(cst, used[0], 0));
+    for (int c = 0; c < 6; ++c) {
+      const int b = c & 1;
+      CK(cudaStreamWaitEvent(cst, used[b], 0));
+      CK(cudaMemcpyAsync(buf[b], comps[c], sizeof(double) * kp.n, cudaMemcpyHostToDevice, cst));
+      CK(cudaEventRecord(copied[b], cst));
+      CK(cudaStreamWaitEvent(st, copied[b], 0));
+      Launch<T>::upload_comp(d, kp, buf[b], c, st);
+      CK(cudaEventRecord(used[b], st));
+    }
+    CK(cudaMemcpyAsync(d.staging_i, flag, sizeof(int32_t) * kp.n, cudaMemcpyHostToDevice, cst));
+    CK(cudaEventRecord(copied[0], cst));
+    CK(cudaStreamWaitEvent(st, copied[0], 0));
+    Launch<T>::upload_flag(d, kp, d.staging_i, st);
     const size_t nb = sizeof(double) * 3 * (size_t)kp.ns;
     if (kp.ns > 0) {
       CK(cudaMemcpyAsync(d.dpos, dpos, nb, cudaMemcpyHostToDevice, st));
@@ -473,16 +503,31 @@ struct Engine : EngineBase {
                double* dpos, double* dvel, double* dforce) override {
     if (advanced) return MPCMD_ERR_STATE;
     flush_shell();
+    // component c is converted into buffer c & 1 on st while component c - 1
+    // is copied out on cst; a buffer is rewritten only after its copy
     double* outs[6] = {x, y, z, vx, vy, vz};
+    double* buf[2] = {d.staging, d.staging2};
+    cudaEvent_t copied[2] = {xev[0], xev[1]}, done[2] = {xev[2], xev[3]};
+    CK(cudaEventRecord(copied[0], cst));
+    CK(cudaEventRecord(copied[1], cst));
+    int k = 0;
     for (int c = 0; c < 6; ++c) {
       if (!outs[c]) continue;
-      Launch<T>::download_convert(d, kp, d.staging, c, time_count, (int)(last_rebuild - last_full), st);
-      CK(cudaMemcpyAsync(outs[c], d.staging, sizeof(double) * kp.n, cudaMemcpyDeviceToHost, st));
+      const int b = k++ & 1;
+      CK(cudaStreamWaitEvent(st, copied[b], 0));
+      Launch<T>::download_convert(d, kp, buf[b], c, time_count, (int)(last_rebuild - last_full), st);
+      CK(cudaEventRecord(done[b], st));
+      CK(cudaStreamWaitEvent(cst, done[b], 0));
+      CK(cudaMemcpyAsync(outs[c], buf[b], sizeof(double) * kp.n, cudaMemcpyDeviceToHost, cst));
+      CK(cudaEventRecord(copied[b], cst));
     }
     if (flag) {
       Launch<T>::download_flag(d, kp, d.staging_i, st);
-      CK(cudaMemcpyAsync(flag, d.staging_i, sizeof(int32_t) * kp.n, cudaMemcpyDeviceToHost, st));
+      CK(cudaEventRecord(done[0], st));
+      CK(cudaStreamWaitEvent(cst, done[0], 0));
+      CK(cudaMemcpyAsync(flag, d.staging_i, sizeof(int32_t) * kp.n, cudaMemcpyDeviceToHost, cst));
     }
+    CK(cudaStreamSynchronize(cst));
     const size_t nb = sizeof(double) * 3 * (size_t)kp.ns;
     if (kp.ns > 0) {
       if (dpos) CK(cudaMemcpyAsync(dpos, d.dpos, nb, cudaMemcpyDeviceToHost, st));

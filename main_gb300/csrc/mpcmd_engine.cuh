@@ -123,6 +123,7 @@ struct Dev {
   uint32_t* scan_tmp;      // scan scratch
   Counters* ctr;
   double* staging;         // host-exchange staging [n]
+  double* staging2;        // second staging buffer (copies overlap conversions)
   int32_t* staging_i;      // [n]
 };
 
@@ -152,9 +153,10 @@ struct StepArgs {
 
 template <typename T>
 struct Launch {
-  static void upload_convert(const Dev<T>& d, const KParams<T>& kp, const double* x, const double* y,
-                             const double* z, const double* vx, const double* vy, const double* vz,
-                             const int32_t* flag, cudaStream_t st);
+  // conversion of one uploaded FP64 component (0-2 positions, 3-5
+  // velocities) or of the int32 flags from a staging buffer
+  static void upload_comp(const Dev<T>& d, const KParams<T>& kp, const double* src, int comp, cudaStream_t st);
+  static void upload_flag(const Dev<T>& d, const KParams<T>& kp, const int32_t* src, cudaStream_t st);
   static void download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
                                int tc_defer, cudaStream_t st);
   static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st);

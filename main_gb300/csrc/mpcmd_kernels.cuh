@@ -226,19 +226,16 @@ __global__ void k_upload_flag(Particles<T> p, KParams<T> kp, const int32_t* f) {
 }
 
 template <typename T>
-void Launch<T>::upload_convert(const Dev<T>& d, const KParams<T>& kp, const double* x, const double* y,
-                               const double* z, const double* vx, const double* vy, const double* vz,
-                               const int32_t* flag, cudaStream_t st) {
+void Launch<T>::upload_comp(const Dev<T>& d, const KParams<T>& kp, const double* src, int comp, cudaStream_t st) {
   const int g = 1024;
-  const double* comps[6] = {x, y, z, vx, vy, vz};
-  for (int c = 0; c < 6; ++c) {
-    cudaMemcpyAsync(d.staging, comps[c], kp.n * sizeof(double), cudaMemcpyHostToDevice, st);
-    if (c < 3) k_upload_pos<T><<<g, TPB, 0, st>>>(d.p, kp, d.staging, c);
-    else k_upload_vel<T><<<g, TPB, 0, st>>>(d.p, kp, d.staging, c - 3);
-    LAUNCH_COUNT();
-  }
-  cudaMemcpyAsync(d.staging_i, flag, kp.n * sizeof(int32_t), cudaMemcpyHostToDevice, st);
-  k_upload_flag<T><<<g, TPB, 0, st>>>(d.p, kp, d.staging_i);
+  if (comp < 3) k_upload_pos<T><<<g, TPB, 0, st>>>(d.p, kp, src, comp);
+  else k_upload_vel<T><<<g, TPB, 0, st>>>(d.p, kp, src, comp - 3);
+  LAUNCH_COUNT();
+}
+
+template <typename T>
+void Launch<T>::upload_flag(const Dev<T>& d, const KParams<T>& kp, const int32_t* src, cudaStream_t st) {
+  k_upload_flag<T><<<1024, TPB, 0, st>>>(d.p, kp, src);
   LAUNCH_COUNT();
 }
 
