@@ -895,7 +895,7 @@ struct Engine : EngineBase {
   int observables(mpcmd_obs* o) override {
     std::memset(o, 0, sizeof(*o));
     CK(cudaMemsetAsync(d.ctr->sums, 0, 8 * sizeof(double), st));
-    Launch<T>::observables(d, kp, cfg.mass, st);
+    Launch<T>::observables(d, kp, cfg.mass, grid, st);
     Counters h;
     int r = read_counters(h);
     if (r) return r;

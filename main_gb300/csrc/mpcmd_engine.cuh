@@ -190,7 +190,7 @@ struct Launch {
   static void flush(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void regather(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
-  static void observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, cudaStream_t st);
+  static void observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, int grid, cudaStream_t st);
   static void concentration(const Dev<T>& d, const KParams<T>& kp, int tc, int tc_defer, const ConcArgs& c,
                             cudaStream_t st);
   // resident blocks per SM of the persistent kernels (rebuild, force, rotate)

@@ -2313,8 +2313,8 @@ __global__ void k_observables(Dev<T> d, KParams<T> kp, double m0, double m1, dou
 }
 
 template <typename T>
-void Launch<T>::observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, cudaStream_t st) {
-  k_observables<T><<<512, TPB, 0, st>>>(d, kp, mass[0], mass[1], mass[2], mass[3]);
+void Launch<T>::observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, int grid, cudaStream_t st) {
+  k_observables<T><<<grid, TPB, 0, st>>>(d, kp, mass[0], mass[1], mass[2], mass[3]);
   LAUNCH_COUNT();
 }
 
