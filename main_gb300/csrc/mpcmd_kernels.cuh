@@ -799,31 +799,34 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
   // GPU still sweeps the arrays front to back, and the near list a warp
   // stages holds particles of one tile at a time, so the shell built from it
   // keeps their spatial (cell) order.
+  // (32-bit indices: particle counts are below 2^31, and an index plus one
+  // tile stride stays below 2^32)
   constexpr int FAR_STEPS = 16;
-  constexpr int64_t FAR_TILE = (int64_t)FAR_STEPS * TPB;
-  const int64_t tile_stride = (int64_t)gridDim.x * FAR_TILE;
-  int64_t i = (int64_t)blockIdx.x * FAR_TILE + threadIdx.x;
+  constexpr uint32_t FAR_TILE = (uint32_t)FAR_STEPS * TPB;
+  const uint32_t n32 = (uint32_t)kp.n;
+  const uint32_t tile_stride = gridDim.x * FAR_TILE;
+  uint32_t i = blockIdx.x * FAR_TILE + threadIdx.x;
   int step = 0;
-  auto advance = [&](int64_t j, int st) -> int64_t {   // the index after j (at step st of its tile)
-    return st + 1 < FAR_STEPS ? j + TPB : j - (int64_t)(FAR_STEPS - 1) * TPB + tile_stride;
+  auto advance = [&](uint32_t j, int st) -> uint32_t {   // the index after j (at step st of its tile)
+    return st + 1 < FAR_STEPS ? j + TPB : j - (uint32_t)(FAR_STEPS - 1) * TPB + tile_stride;
   };
   uint8_t pf_f = FLAG_HOME_SHELL;
   uint32_t pf_cell = 0;
   T pf_ox = 0, pf_oy = 0, pf_oz = 0, pf_vx = 0, pf_vy = 0, pf_vz = 0;
-  if (i < kp.n) {
+  if (i < n32) {
     pf_f = d.p.flag[i]; pf_cell = d.p.cell[i];
     pf_ox = d.p.ox[i]; pf_oy = d.p.oy[i]; pf_oz = d.p.oz[i];
     pf_vx = d.p.vx[i]; pf_vy = d.p.vy[i]; pf_vz = d.p.vz[i];
   }
   // the loop runs while the warp's step base is inside the array (warp-uniform)
-  for (; i - lane < kp.n; i = advance(i, step), step = step + 1 < FAR_STEPS ? step + 1 : 0) {
-    const bool in = i < kp.n;
+  for (; i - lane < n32; i = advance(i, step), step = step + 1 < FAR_STEPS ? step + 1 : 0) {
+    const bool in = i < n32;
     const uint8_t f = pf_f;
     uint32_t cell = pf_cell;
     T ox = pf_ox, oy = pf_oy, oz = pf_oz;
     T vx = pf_vx, vy = pf_vy, vz = pf_vz;
-    const int64_t inext = advance(i, step);
-    if (inext < kp.n) {
+    const uint32_t inext = advance(i, step);
+    if (inext < n32) {
       pf_f = d.p.flag[inext]; pf_cell = d.p.cell[inext];
       pf_ox = d.p.ox[inext]; pf_oy = d.p.oy[inext]; pf_oz = d.p.oz[inext];
       pf_vx = d.p.vx[inext]; pf_vy = d.p.vy[inext]; pf_vz = d.p.vz[inext];
@@ -2047,16 +2050,18 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
   // blocks take tiles of ROT_TILE consecutive particles in a grid stride (two
   // 256-particle steps per iteration), so that the watch list a warp stages
   // keeps the particles' cell order
+  // (32-bit indices: particle counts are below 2^31)
   constexpr int ROT_STEPS = 16;
-  constexpr int64_t ROT_TILE = (int64_t)ROT_STEPS * TPB;
-  const int64_t tile_stride = (int64_t)gridDim.x * ROT_TILE;
+  constexpr uint32_t ROT_TILE = (uint32_t)ROT_STEPS * TPB;
+  const uint32_t n32 = (uint32_t)kp.n;
+  const uint32_t tile_stride = gridDim.x * ROT_TILE;
   int step = 0;
-  for (int64_t i0 = (int64_t)blockIdx.x * ROT_TILE + threadIdx.x; i0 - lane < kp.n;
-       i0 = step + 2 < ROT_STEPS ? i0 + 2 * TPB : i0 - (int64_t)(ROT_STEPS - 2) * TPB + tile_stride,
+  for (uint32_t i0 = blockIdx.x * ROT_TILE + threadIdx.x; i0 - lane < n32;
+       i0 = step + 2 < ROT_STEPS ? i0 + 2 * TPB : i0 - (uint32_t)(ROT_STEPS - 2) * TPB + tile_stride,
        step = step + 2 < ROT_STEPS ? step + 2 : 0) {
-    const int64_t i1 = i0 + TPB;
-    const bool h0 = i0 < kp.n;
-    const bool h1 = i1 < kp.n;
+    const uint32_t i1 = i0 + TPB;
+    const bool h0 = i0 < n32;
+    const bool h1 = i1 < n32;
     bool w0 = false, w1 = false;
     const uint8_t f0 = h0 ? d.p.flag[i0] : FLAG_HOME_SHELL;
     const uint8_t f1 = h1 ? d.p.flag[i1] : FLAG_HOME_SHELL;
