@@ -32,6 +32,7 @@ constexpr uint8_t FLAG_HOME_SHELL = 0x40;
 constexpr int PAIRMAX = 8;         // spheres one shell particle may interact with
 constexpr int BIN_SLOTS = 16;      // spheres one coarse bin may list
 constexpr int BIN_EDGE = 4;        // coarse bin edge in cells
+constexpr int GAP_EDGE = 2;        // gap-field bin edge in cells (watch list)
 
 // ---------------------------------------------------------------- Philox --
 // Philox4x32-10 (Salmon et al., SC'11): counter (index, extra, step, tag),
@@ -130,6 +131,7 @@ struct KParams {
   float kf[6], tauf;      // the same rounded to float (FP32 reaction path)
   double dtd;            // MD step in FP64
   int nbx, nby, nbz;     // coarse sphere-bin grid
+  int ngx, ngy, ngz;     // gap-field grid (GAP_EDGE cells per bin edge)
   // dimer constants (FP64): sphere-sphere LJ by pair type [CC, CN, NN]
   double Ld[3];
   double mot_cut2[3], mot_R6[3], mot_R12[3], mot_r6R6[3], mot_r12R12[3];

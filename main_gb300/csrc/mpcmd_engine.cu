@@ -333,6 +333,9 @@ struct Engine : EngineBase {
     kp.nbx = (c.lx + BIN_EDGE - 1) / BIN_EDGE;
     kp.nby = (c.ly + BIN_EDGE - 1) / BIN_EDGE;
     kp.nbz = (c.lz + BIN_EDGE - 1) / BIN_EDGE;
+    kp.ngx = (c.lx + GAP_EDGE - 1) / GAP_EDGE;
+    kp.ngy = (c.ly + GAP_EDGE - 1) / GAP_EDGE;
+    kp.ngz = (c.lz + GAP_EDGE - 1) / GAP_EDGE;
     const double msum[3] = {c.rc + c.rc + c.rm_delta, c.rc + c.rn + c.rm_delta, c.rn + c.rn + c.rm_delta};
     for (int t = 0; t < 3; ++t) {
       double r2 = msum[t] * msum[t], R6 = r2 * r2 * r2, R12 = R6 * R6;
@@ -373,7 +376,7 @@ struct Engine : EngineBase {
     int64_t nbins = (int64_t)kp.nbx * kp.nby * kp.nbz;
     r |= alloc(d.bin_cnt, nbins); r |= alloc(d.bin_list, nbins * BIN_SLOTS);
     r |= alloc(d.bin_mask, (nbins + 31) / 32);
-    r |= alloc(d.gapf, nbins); r |= alloc(d.watch, n);
+    r |= alloc(d.gapf, (int64_t)kp.ngx * kp.ngy * kp.ngz); r |= alloc(d.watch, n);
     r |= alloc(d.sph_cnt, ns1 * SHELL_CLASSES); r |= alloc(d.sph_base, ns1 * SHELL_CLASSES);
     if (sizeof(T) == 4) { float4* a = nullptr; r |= alloc(a, kp.ncell_shift); d.acc = a; }
     else { double* a = nullptr; r |= alloc(a, 4 * kp.ncell_shift); d.acc = a; }

@@ -498,6 +498,11 @@ __device__ __forceinline__ int bin_of(int lx, int ly, int nbx, int nby, uint32_t
   return cell_x(cell) / BIN_EDGE + nbx * (cell_y(cell) / BIN_EDGE + nby * (cell_z(cell) / BIN_EDGE));
 }
 
+// Gap-field bin of a cell (GAP_EDGE cells per bin edge).
+__device__ __forceinline__ int gap_bin_of(int ngx, int ngy, uint32_t cell) {
+  return cell_x(cell) / GAP_EDGE + ngx * (cell_y(cell) / GAP_EDGE + ngy * (cell_z(cell) / GAP_EDGE));
+}
+
 // Bins whose bitmask fits in shared memory (32 KB: a 256^3-cell box).
 constexpr int BIN_MASK_SMEM_WORDS = 8192;
 
@@ -1973,42 +1978,47 @@ __global__ void k_gap_fill(Dev<T> d, KParams<T> kp, double Rc, double Rn, int ho
   const double vmax = sqrt(__longlong_as_double((long long)d.ctr->vlast));
   const double vs = (double)sphere_speed_bound<T>(d.ctr);
   const double reach = (3.0 * vmax + vs) * kp.dtd * (double)horizon + 1.0;
-  const double hd = 0.5 * sqrt(3.0) * (double)BIN_EDGE;
+  const double hd = 0.5 * sqrt(3.0) * (double)GAP_EDGE;
   const double Rm = Rl + reach + hd;
-  const int nb[3] = {kp.nbx, kp.nby, kp.nbz};
+  const int nb[3] = {kp.ngx, kp.ngy, kp.ngz};
   const double L[3] = {(double)kp.lx, (double)kp.ly, (double)kp.lz};
   const bool per[3] = {true, true, kp.geometry == 1};
   double X[3];
   int lo[3], hi[3];
   for (int q = 0; q < 3; ++q) {
     X[q] = d.dpos[3 * s + q];
-    lo[q] = (int)floor((X[q] - Rm) / (double)BIN_EDGE);
-    hi[q] = (int)floor((X[q] + Rm) / (double)BIN_EDGE);
+    lo[q] = (int)floor((X[q] - Rm) / (double)GAP_EDGE);
+    hi[q] = (int)floor((X[q] + Rm) / (double)GAP_EDGE);
     if (!per[q]) { lo[q] = max(lo[q], 0); hi[q] = min(hi[q], nb[q] - 1); }
     else if (hi[q] - lo[q] + 1 >= nb[q]) { lo[q] = 0; hi[q] = nb[q] - 1; }
   }
   const int n0 = hi[0] - lo[0] + 1, n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1;
   const int tot = n0 * n1 * n2;
+  // the per-bin arithmetic in FP32 (FP64 is slow on this part), with a
+  // margin of 1e-3 cells that keeps the bound below the exact one
+  const float Xf[3] = {(float)X[0], (float)X[1], (float)X[2]};
+  const float Lf[3] = {(float)L[0], (float)L[1], (float)L[2]};
+  const float sub = (float)(hd + Rl) + 1e-3f;
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     int w[3] = {lo[0] + t % n0, lo[1] + (t / n0) % n1, lo[2] + t / (n0 * n1)};
-    double d2 = 0.0;
+    float d2 = 0.f;
     for (int q = 0; q < 3; ++q) {
-      if (per[q]) w[q] = ((w[q] % nb[q]) + nb[q]) % nb[q];
-      double dc = (double)w[q] * BIN_EDGE + 0.5 * BIN_EDGE - X[q];
-      if (per[q]) dc = dmin_image(dc, L[q]);
+      if (per[q]) { if (w[q] < 0) w[q] += nb[q]; else if (w[q] >= nb[q]) w[q] -= nb[q]; }
+      float dc = (float)(w[q] * GAP_EDGE) + 0.5f * (float)GAP_EDGE - Xf[q];
+      if (per[q]) dc = min_image(dc, Lf[q]);
       d2 += dc * dc;
     }
-    double lb = sqrt(d2) - hd - Rl;
-    if (lb < 0.0) lb = 0.0;
+    float lb = sqrtf(d2) - sub;
+    if (lb < 0.f) lb = 0.f;
     const int b = w[0] + nb[0] * (w[1] + nb[1] * w[2]);
     if (!chk(b >= 0 && b < nb[0] * nb[1] * nb[2], d.ctr, 122, b)) continue;
-    atomicMin(&d.gapf[b], __float_as_uint((float)lb));
+    atomicMin(&d.gapf[b], __float_as_uint(lb));
   }
 }
 
 template <typename T>
 void Launch<T>::gap_field(const Dev<T>& d, const KParams<T>& kp, int horizon, cudaStream_t st) {
-  const int nbins = kp.nbx * kp.nby * kp.nbz;
+  const int nbins = kp.ngx * kp.ngy * kp.ngz;
   cudaMemsetAsync(d.gapf, 0x7F, sizeof(uint32_t) * nbins, st);   // 3.4e38
   if (kp.ns == 0) return;
   const double Rc = sqrt((double)kp.full2[0]) + 1e-6, Rn = sqrt((double)kp.full2[1]) + 1e-6;
@@ -2086,8 +2096,8 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
     }
     T g0 = (T)3e38, g1 = (T)3e38;
     if (a.watch_build) {
-      if (r0) g0 = __uint_as_float(d.gapf[bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, c0)]);
-      if (r1) g1 = __uint_as_float(d.gapf[bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, c1)]);
+      if (r0) g0 = __uint_as_float(d.gapf[gap_bin_of(kp.ngx, kp.ngy, c0)]);
+      if (r1) g1 = __uint_as_float(d.gapf[gap_bin_of(kp.ngx, kp.ngy, c1)]);
     }
     if (r0) {
       rotate_v(kp, t0, vx0, vy0, vz0);
