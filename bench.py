@@ -54,6 +54,24 @@ def rank_info():
     return ws, rk, lr
 
 
+def max_over_ranks(x, dist, device="cuda"):
+    """The largest of each rank's x (every rank gets it); x itself without a
+    process group.  `device`: where the reduction tensor lives (cuda for
+    NCCL, cpu for gloo)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(ws, n_per_rank, md_steps, periods, seconds):
+    """Whole-job particle-steps/s of ws replicas that each advanced n_per_rank
+    particles by md_steps x periods MD steps, timed by the slowest rank."""
+    return ws * n_per_rank * md_steps * periods / seconds
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
 
@@ -202,12 +220,8 @@ def gpu_arm(args, ws, rk, lr, dist):
         launches = main_gb300.kernel_launches() - l0
     barrier()
     clocks = ck.summary()
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * N * S * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(ms, dist)
+    value = aggregate_rate(ws, N, S, args.steps, ms * 1e-3)
 
     # pass B: per-launch timing of each kernel kind over the same kind of region
     e.profile(True)
@@ -274,12 +288,8 @@ def gpu_arm(args, ws, rk, lr, dist):
         state_bytes = N * (6 * 8 + 4) + ns * 3 * 8 * 3
         obs_bytes = 8 * 16 + ns * 3 * 8 + cfg["n_dimers"] * 8
         e2e_s = t1 - t0
-        if dist is not None:
-            import torch
-            t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": ws * N * S * args.steps / e2e_s, "unit": UNIT,
+        e2e_s = max_over_ranks(e2e_s, dist)
+        e2e = {"value": aggregate_rate(ws, N, S, args.steps, e2e_s), "unit": UNIT,
                "h2d_bytes_per_step": int(state_bytes / args.steps),
                "d2h_bytes_per_step": int((state_bytes + args.steps * obs_bytes) / args.steps),
                "pinned_host": pinned,
