@@ -1960,7 +1960,7 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
 
 template <typename T>
 void Launch<T>::cells(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int what, cudaStream_t st) {
-  k_cells<T><<<a.grid, TPB, 0, st>>>(d, kp, a, what);
+  k_cells<T><<<a.g_cells > 0 ? a.g_cells : a.grid, TPB, 0, st>>>(d, kp, a, what);
   LAUNCH_COUNT();
 }
 
@@ -2140,11 +2140,12 @@ void Launch<T>::rotate_main(const Dev<T>& d, const KParams<T>& kp, const StepArg
 
 template <typename T>
 void Launch<T>::occupancy(int* blocks) {
-  blocks[0] = blocks[1] = blocks[2] = blocks[3] = 0;
+  blocks[0] = blocks[1] = blocks[2] = blocks[3] = blocks[4] = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], k_rebuild<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], k_force<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], k_rotate_main<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], k_rebuild_far<T>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[4], k_cells<T>, TPB, 0);
 }
 
 // ---------------------------------------------------- shell home moves ----
