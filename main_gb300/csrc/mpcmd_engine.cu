@@ -177,7 +177,7 @@ struct Engine : EngineBase {
   cudaStream_t cst = nullptr;
   cudaEvent_t xev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<void*> allocs;
-  int grid = 0, g_rebuild = 0, g_force = 0, g_rotate = 0, g_far = 0, g_cells = 0;
+  int grid = 0, g_rebuild = 0, g_force = 0, g_rotate = 0, g_far = 0, g_cells = 0, g_shell = 0;
   int64_t cstep = 0;
   int time_count = 0, time_penetrate = 0;
   int64_t last_rebuild = 0;
@@ -282,7 +282,7 @@ struct Engine : EngineBase {
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     grid = nsm * 8;
     // the heavy persistent kernels run exactly one wave: SMs x resident blocks
-    int occ[5];
+    int occ[6];
     Launch<T>::occupancy(occ);
     CK(cudaGetLastError());
     g_rebuild = nsm * std::max(occ[0], 1);
@@ -290,6 +290,7 @@ struct Engine : EngineBase {
     g_rotate = nsm * std::max(occ[2], 1);
     g_far = nsm * std::max(occ[3], 1);
     g_cells = nsm * std::max(occ[4], 1);
+    g_shell = nsm * std::max(occ[5], 1);
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking));
     for (cudaEvent_t& e : xev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -546,7 +547,7 @@ struct Engine : EngineBase {
     StepArgs a{};
     a.step = (uint32_t)step;
     a.grid = grid;
-    a.g_rebuild = g_rebuild; a.g_force = g_force; a.g_rotate = g_rotate; a.g_far = g_far; a.g_cells = g_cells;
+    a.g_rebuild = g_rebuild; a.g_force = g_force; a.g_rotate = g_rotate; a.g_far = g_far; a.g_cells = g_cells; a.g_shell = g_shell;
     a.shift[0] = shift[0]; a.shift[1] = shift[1]; a.shift[2] = shift[2];
     for (int c = 0; c < 3; ++c) a.shf[c] = (float)shift[c];
     return a;

@@ -143,6 +143,7 @@ struct StepArgs {
   int g_rotate;
   int g_far;           // SMs x resident blocks of k_rebuild_far
   int g_cells;         // SMs x resident blocks of k_cells (one wave)
+  int g_shell;         // SMs x resident blocks of k_shell_advance (one wave)
   int watch_build;     // > 0 (the period in steps): rotate_main / rotate_shell build the watch list
   int use_watch;       // a rebuild between full passes visits the watch list only
   int near;            // the rebuild visits the particles the far pass deferred (list in `watch`)

@@ -1231,7 +1231,7 @@ __global__ void k_shell_commit(Counters* c, int64_t cap) {
 
 template <typename T>
 void Launch<T>::advance(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
-  k_shell_advance<T><<<a.grid, TPB, 0, st>>>(d, kp, a, 0);
+  k_shell_advance<T><<<a.g_shell > 0 ? a.g_shell : a.grid, TPB, 0, st>>>(d, kp, a, 0);
   LAUNCH_COUNT();
   if (a.advance && a.horizon > 0) {
     k_shell_commit<T><<<1, 1, 0, st>>>(d.ctr, d.sh2.cap);
@@ -1241,7 +1241,7 @@ void Launch<T>::advance(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a
 
 template <typename T>
 void Launch<T>::rotate_shell(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
-  k_shell_advance<T><<<a.grid, TPB, 0, st>>>(d, kp, a, 1);
+  k_shell_advance<T><<<a.g_shell > 0 ? a.g_shell : a.grid, TPB, 0, st>>>(d, kp, a, 1);
   LAUNCH_COUNT();
   if (a.advance && a.horizon > 0) {
     k_shell_commit<T><<<1, 1, 0, st>>>(d.ctr, d.sh2.cap);
@@ -2140,12 +2140,13 @@ void Launch<T>::rotate_main(const Dev<T>& d, const KParams<T>& kp, const StepArg
 
 template <typename T>
 void Launch<T>::occupancy(int* blocks) {
-  blocks[0] = blocks[1] = blocks[2] = blocks[3] = blocks[4] = 0;
+  blocks[0] = blocks[1] = blocks[2] = blocks[3] = blocks[4] = blocks[5] = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], k_rebuild<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], k_force<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], k_rotate_main<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], k_rebuild_far<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[4], k_cells<T>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[5], k_shell_advance<T>, TPB, 0);
 }
 
 // ---------------------------------------------------- shell home moves ----
