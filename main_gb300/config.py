@@ -217,7 +217,7 @@ def workload(name, scale=1.0, **kw):
                     exclusion=EXCL_CELLS, catalysis=CAT_PROBABILISTIC, rotation_sense=-1,
                     cell_capacity=200, n_solvent=n, init_count=[nf, ng, 0, n - nf - ng],
                     eps_c=[1.0, 1.0, 0.0, 1.0], eps_n=[1.0, 0.1, 0.0, 1.0],
-                    k=[1.0, 0.1, 1.0, 0.0, 0.01, 0.0], sort_every=5000)
+                    k=[1.0, 0.1, 1.0, 0.0, 0.01, 0.0], sort_every=10000)
     else:
         raise ValueError("unknown workload %r" % name)
     if "n_solvent" in kw and "init_count" not in kw and name == "c2":
