@@ -1023,10 +1023,12 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
     const bool act = j < (int64_t)nin;
     uint32_t cell = 0, idx = 0;
     T ox = 0, oy = 0, oz = 0, vx = 0, vy = 0, vz = 0;
+    T msd0 = (T)0;   // loaded with the rest: its use at the end would wait on it
     uint8_t fl = 0;
     int np = 0;
     uint16_t sphl[PAIRMAX];
     if (act) {
+      if (a.advance && !a.mpc) msd0 = d.sh.msd[j];
       cell = d.sh.cell[j];
       ox = d.sh.ox[j]; oy = d.sh.oy[j]; oz = d.sh.oz[j];
       vx = d.sh.vx[j]; vy = d.sh.vy[j]; vz = d.sh.vz[j];
@@ -1097,7 +1099,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
           vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
         }
         stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
-        T msd = d.sh.msd[j] + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
+        T msd = msd0 + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
         d.sh.msd[j] = msd;
         msdmax = msd > msdmax ? msd : msdmax;
         d.sh.cell[j] = cell;
