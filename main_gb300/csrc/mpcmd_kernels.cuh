@@ -125,20 +125,20 @@ __device__ __forceinline__ void warp_sphere_add(double* facc, int s, T fx, T fy,
     const int src = __ffs(remaining) - 1;
     const int sr = __shfl_sync(full, s, src);
     const unsigned grp = __ballot_sync(full, s == sr);
-    T a0 = s == sr ? fx : (T)0, a1 = s == sr ? fy : (T)0, a2 = s == sr ? fz : (T)0, a3 = s == sr ? u : (T)0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a0 += __shfl_xor_sync(full, a0, o);
-      a1 += __shfl_xor_sync(full, a1, o);
-      a2 += __shfl_xor_sync(full, a2, o);
-      a3 += __shfl_xor_sync(full, a3, o);
-    }
-    if (lane == src) {
-      atomicAdd(&facc[4 * sr + 0], to_f64(a0));
-      atomicAdd(&facc[4 * sr + 1], to_f64(a1));
-      atomicAdd(&facc[4 * sr + 2], to_f64(a2));
-      atomicAdd(&facc[4 * sr + 3], to_f64(a3));
-    }
+    const T a0 = s == sr ? fx : (T)0, a1 = s == sr ? fy : (T)0, a2 = s == sr ? fz : (T)0, a3 = s == sr ? u : (T)0;
+    // transposing reduction: the first two levels halve the values a lane
+    // carries (6 shuffles for the four sums instead of 20); lane 8v ends with
+    // the warp total of value v
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+    T k0 = h16 ? a2 : a0, k1 = h16 ? a3 : a1;
+    k0 += __shfl_xor_sync(full, h16 ? a0 : a2, 16);
+    k1 += __shfl_xor_sync(full, h16 ? a1 : a3, 16);
+    T k = h8 ? k1 : k0;
+    k += __shfl_xor_sync(full, h8 ? k0 : k1, 8);
+    k += __shfl_xor_sync(full, k, 4);
+    k += __shfl_xor_sync(full, k, 2);
+    k += __shfl_xor_sync(full, k, 1);
+    if ((lane & 7) == 0) atomicAdd(&facc[4 * sr + (lane >> 3)], to_f64(k));
     remaining &= ~grp;
   }
 }
