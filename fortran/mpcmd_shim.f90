@@ -59,7 +59,12 @@ module mpcmd_shim
     real(c_double) :: k(6)
     integer(c_int32_t) :: precision
     integer(c_int32_t) :: shell_capacity
-    integer(c_int32_t) :: reserved(6)
+    integer(c_int32_t) :: variant
+    integer(c_int32_t) :: layout
+    integer(c_int32_t) :: layout_rows, layout_cols
+    integer(c_int32_t) :: reserved(2)
+    real(c_double) :: tether_k, tether_z
+    real(c_double) :: layout_sep
   end type mpcmd_config
 
   ! struct mpcmd_conc_params
@@ -84,7 +89,7 @@ module mpcmd_shim
   public :: mpcmd_set_step, mpcmd_initial, mpcmd_prepare, mpcmd_step, mpcmd_evolve, mpcmd_run
   public :: mpcmd_sort, mpcmd_rebuild_lists, mpcmd_distribute, mpcmd_mpc_rotation, mpcmd_reaction
   public :: mpcmd_observables, mpcmd_checkpoint, mpcmd_restore, mpcmd_set_cell_order
-  public :: mpcmd_concentration, mpcmd_dimer_axes
+  public :: mpcmd_concentration, mpcmd_dimer_axes, mpcmd_set_anchors, mpcmd_get_anchors
   public :: mpcmd_check
 
   interface
@@ -120,6 +125,17 @@ module mpcmd_shim
       real(c_double), intent(out) :: x(*), y(*), z(*), vx(*), vy(*), vz(*)
       integer(c_int32_t), intent(out) :: flag(*)
       real(c_double), intent(out) :: dpos(*), dvel(*), dforce(*)
+    end function
+    ! motorCM of rotational_code/2d_array (main_rotation.f95:89), [3, numdims]
+    integer(c_int) function mpcmd_set_anchors(ctx, anchors) bind(C, name="mpcmd_set_anchors")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: anchors(*)
+    end function
+    integer(c_int) function mpcmd_get_anchors(ctx, anchors) bind(C, name="mpcmd_get_anchors")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: anchors(*)
     end function
     integer(c_int) function mpcmd_set_cell_order(ctx, order, n) bind(C, name="mpcmd_set_cell_order")
       import :: c_int, c_ptr, c_int32_t, c_int64_t

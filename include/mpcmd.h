@@ -41,6 +41,14 @@ enum { MPCMD_KIN_NONE = 0, MPCMD_KIN_SIMPLE = 1, MPCMD_KIN_SELKOV = 2 };
 enum { MPCMD_EXCL_PARTICLE = 0, MPCMD_EXCL_CELLS = 1 };
 enum { MPCMD_CAT_DETERMINISTIC = 0, MPCMD_CAT_PROBABILISTIC = 1 };
 enum { MPCMD_PREC_FP32 = 32, MPCMD_PREC_FP64 = 64 };
+/* rotational_code variants: MOTOR is the free dimer of collective_code and
+ * selkov_code; ROTOR is the anchored dimer of rotational_code/2d_array and
+ * linear_periodic_ci (see `variant` below).  Layouts of mpcmd_initial: random
+ * placement (initial_mod.f95:78-119), a rows x cols grid
+ * (rotational_code/2d_array/initial_mod.f95:68-90) or a line along x
+ * (rotational_code/linear_periodic_ci/initial_mod.f95:72-88). */
+enum { MPCMD_VARIANT_MOTOR = 0, MPCMD_VARIANT_ROTOR = 1 };
+enum { MPCMD_LAYOUT_RANDOM = 0, MPCMD_LAYOUT_GRID = 1, MPCMD_LAYOUT_LINE = 2 };
 
 /* Run configuration.  The first block (through k[6]) carries the reference
  * input decks (collective_code/input.txt read at main_pattern.f95:19-64,
@@ -79,7 +87,17 @@ typedef struct mpcmd_config {
   /* GB300 engine options (not in the reference decks). */
   int32_t precision;         /* MPCMD_PREC_FP32 (default) or MPCMD_PREC_FP64         */
   int32_t shell_capacity;    /* 0 = sized from the sphere shells                     */
-  int32_t reserved[6];
+  /* rotational_code variants (rotational_code/2d_array/main_rotation.f95:17-69). */
+  int32_t variant;           /* MPCMD_VARIANT_ROTOR: every dimer's midpoint is held at
+                                its anchor (RATTLE of 2d_array/evolve_mod.f95:283-391,
+                                596-650), a harmonic z tether on each sphere
+                                (forces_mod.f95:177-201) replaces the 9-3 wall, and
+                                there is no motor-motor LJ                          */
+  int32_t layout;            /* MPCMD_LAYOUT_*: dimer placement of mpcmd_initial     */
+  int32_t layout_rows, layout_cols;  /* numrows, numcols of the grid layout          */
+  int32_t reserved[2];
+  double tether_k, tether_z; /* k_harm, zdimeq (= Rc + gap)                          */
+  double layout_sep;         /* sep: gap between neighbouring motors of a layout     */
 } mpcmd_config;
 
 typedef struct mpcmd_obs {
@@ -113,6 +131,13 @@ int mpcmd_download_state(mpcmd_ctx* ctx, double* x, double* y, double* z,
  * order[k] = 0-based row-major id of the k-th cell.  Without it the engine
  * uses its own Hilbert order. */
 int mpcmd_set_cell_order(mpcmd_ctx* ctx, const int32_t* order, int64_t n);
+/* Anchors of the rotor variant, motorCM [3*n_dimers]
+ * (rotational_code/2d_array/initial_mod.f95:86-88, restart_mod.f95 reads them
+ * back from motor_positions.dat).  mpcmd_initial and mpcmd_upload_state set
+ * them to the midpoints 0.5 (X_C + X_N) of the dimers they place or receive;
+ * mpcmd_restore sets the checkpointed ones. */
+int mpcmd_set_anchors(mpcmd_ctx* ctx, const double* anchors);
+int mpcmd_get_anchors(mpcmd_ctx* ctx, double* anchors);
 int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count);
 
 /* Reference call surface ----------------------------------------------- */

@@ -62,6 +62,8 @@ SIGNATURES = {
     "mpcmd_upload_state": (C.c_int, [_P, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
     "mpcmd_download_state": (C.c_int, [_P, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
     "mpcmd_set_cell_order": (C.c_int, [_P, _ip, C.c_int64]),
+    "mpcmd_set_anchors": (C.c_int, [_P, _dp]),
+    "mpcmd_get_anchors": (C.c_int, [_P, _dp]),
     "mpcmd_set_step": (C.c_int, [_P, C.c_int64, C.c_int32]),
     "mpcmd_initial": (C.c_int, [_P]),
     "mpcmd_prepare": (C.c_int, [_P]),
@@ -205,6 +207,18 @@ class Engine:
     def set_cell_order(self, order):
         a = np.ascontiguousarray(order, dtype=np.int32)
         self._c(lib().mpcmd_set_cell_order(self.h, _ptr(a, C.c_int32), a.size), "set_cell_order")
+
+    def set_anchors(self, anchors):
+        """Rotor anchors (motorCM), one row of three per dimer."""
+        a = np.ascontiguousarray(anchors, dtype=np.float64).reshape(-1, 3)
+        if a.shape[0] != self.ns // 2:
+            raise ValueError("anchors: one row per dimer")
+        self._c(lib().mpcmd_set_anchors(self.h, _ptr(a, C.c_double)), "set_anchors")
+
+    def get_anchors(self):
+        a = np.zeros((max(self.ns // 2, 1), 3))
+        self._c(lib().mpcmd_get_anchors(self.h, _ptr(a, C.c_double)), "get_anchors")
+        return a[: self.ns // 2]
 
     def cell_order(self):
         a = np.zeros(self.ncell, dtype=np.int32)

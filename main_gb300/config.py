@@ -30,7 +30,9 @@ FIELDS = [
     ("rc", _D), ("rn", _D), ("dcn", _D), ("mc", _D), ("mn", _D), ("rw", _D), ("ew", _D),
     ("rm_delta", _D), ("em", _D), ("rp_ab", _D), ("rp_ba", _D), ("kT", _D), ("skin", _D),
     ("rot_angle", _D), ("md_dt", _D), ("mpc_dt", _D), ("k", _D * 6),
-    ("precision", _I32), ("shell_capacity", _I32), ("reserved", _I32 * 6),
+    ("precision", _I32), ("shell_capacity", _I32),
+    ("variant", _I32), ("layout", _I32), ("layout_rows", _I32), ("layout_cols", _I32),
+    ("reserved", _I32 * 2), ("tether_k", _D), ("tether_z", _D), ("layout_sep", _D),
 ]
 
 GEOM_WALLS, GEOM_PERIODIC = 0, 1
@@ -38,6 +40,8 @@ KIN_NONE, KIN_SIMPLE, KIN_SELKOV = 0, 1, 2
 EXCL_PARTICLE, EXCL_CELLS = 0, 1
 CAT_DETERMINISTIC, CAT_PROBABILISTIC = 0, 1
 PREC_FP32, PREC_FP64 = 32, 64
+VARIANT_MOTOR, VARIANT_ROTOR = 0, 1
+LAYOUT_RANDOM, LAYOUT_GRID, LAYOUT_LINE = 0, 1, 2
 
 
 class MpcmdConfig(C.Structure):
@@ -77,7 +81,8 @@ def base_config(**kw):
         rc=4.0, rn=2.0, dcn=6.5, mc=0.0, mn=0.0, rw=1.0, ew=1.0, rm_delta=1.0, em=1.0,
         rp_ab=1.0, rp_ba=0.0, kT=1.0 / 6.0, skin=1.5, rot_angle=2.0 * math.pi / 3.0,
         md_dt=0.01, mpc_dt=0.5, k=[0.01, 0, 0, 0, 0, 0],
-        precision=PREC_FP32, shell_capacity=0, reserved=[0] * 6,
+        precision=PREC_FP32, shell_capacity=0, variant=VARIANT_MOTOR, layout=LAYOUT_RANDOM, layout_rows=0,
+        layout_cols=0, reserved=[0] * 2, tether_k=0.0, tether_z=0.0, layout_sep=0.0,
     )
     cfg.update(kw)
     return finish(cfg)
@@ -108,6 +113,19 @@ SELKOV_KEYS = [
     "seed", "Nf0", "Ng0", "Ni0", "box1", "box2", "box3", "Mf", "Mg", "Mi", "Rc", "Rn", "Dcn",
     "EfC", "EgC", "EiC", "EfN", "EgN", "EiN", "RPfg", "RPgf", "T", "A0", "MDt", "MPCt",
     "k1", "k2", "k3", "k4", "k5", "k6", "Freq1", "Freq2", "Freq3", "Freq4", "Freq5", "Freq6",
+]
+
+# rotational_code/2d_array/main_rotation.f95:17-51 and
+# rotational_code/linear_periodic_ci/main_rotation.f95:17-49
+ROTATIONAL_GRID_KEYS = [
+    "seed", "tstep", "rhoa", "rhob", "box1", "box2", "box3", "sep", "numrows", "numcols", "Ma", "Mb",
+    "Rc", "Rn", "Dcn", "EaC", "EbC", "EaN", "EbN", "k_harm", "gap", "RPab", "RPba", "T", "skinrad",
+    "a0", "rotang", "MDt", "MPCt", "sort_step", "k1", "Freq1", "Freq2", "Freq3", "Freq4",
+]
+ROTATIONAL_LINE_KEYS = [
+    "seed", "tstep", "rhoa", "rhob", "box1", "box2", "box3", "numdims", "Ma", "Mb",
+    "Rc", "Rn", "Dcn", "EaC", "EbC", "EaN", "EbN", "k_harm", "gap", "RPab", "RPba", "T", "skinrad",
+    "a0", "rotang", "MDt", "MPCt", "sort_step", "k1", "Freq1", "Freq2", "Freq3", "Freq4",
 ]
 
 
@@ -161,7 +179,51 @@ def collective_config(deck, **kw):
         rc=deck["Rc"], rn=deck["Rn"], dcn=deck["Dcn"], mc=mc, mn=mn, rw=deck["Rw"], ew=deck["Ew"],
         rm_delta=deck["Rm_delta"], em=deck["Em"], rp_ab=deck["RPab"], rp_ba=deck["RPba"], kT=deck["T"],
         skin=deck["skinrad"], rot_angle=deck["rotang"], md_dt=deck["MDt"], mpc_dt=deck["MPCt"],
-        k=[deck["k1"], 0, 0, 0, 0, 0], precision=PREC_FP32, shell_capacity=0, reserved=[0] * 6,
+        k=[deck["k1"], 0, 0, 0, 0, 0], precision=PREC_FP32, shell_capacity=0, reserved=[0] * 2,
+    )
+    cfg.update(kw)
+    return cfg
+
+
+def read_rotational_input(path, layout=LAYOUT_GRID):
+    return read_deck(path, ROTATIONAL_GRID_KEYS if layout == LAYOUT_GRID else ROTATIONAL_LINE_KEYS)
+
+
+def rotational_config(deck, layout=LAYOUT_GRID, **kw):
+    """rotational_code/2d_array/main_rotation.f95:53-110 (grid of rotors) or
+    linear_periodic_ci/main_rotation.f95:51-108 (line of rotors, sep derived
+    at :52): anchored dimers with a harmonic z tether over a walled box, no
+    motor-motor LJ, no reactive floor, reaction_simple with the rate k1."""
+    box = [int(deck["box1"]), int(deck["box2"]), int(deck["box3"])]
+    vol = box[0] * box[1] * box[2]
+    cutoff = 2.0 ** (1.0 / 6.0)
+    if layout == LAYOUT_GRID:
+        rows, cols = int(deck["numrows"]), int(deck["numcols"])
+        nd = rows * cols
+        sep = deck["sep"]
+    else:
+        rows, cols = 0, 0
+        nd = int(deck["numdims"])
+        sep = (deck["box1"] - nd * (2.0 * deck["Rc"] * cutoff + deck["Dcn"])) / nd
+    # Vact as the drivers compute it (the N-sphere volume enters with a minus)
+    vact = vol - nd * ((4.0 * math.pi * deck["Rc"] ** 3) / 3.0 - (4.0 * math.pi * deck["Rn"] ** 3) / 3.0)
+    na0 = math.floor(deck["rhoa"] * vact)
+    nb0 = math.floor(deck["rhob"] * vact)
+    nt = na0 + nb0
+    mc, mn = sphere_masses(nt, vol, deck["Rc"], deck["Rn"])
+    cfg = dict(
+        lx=box[0], ly=box[1], lz=box[2], geometry=GEOM_WALLS, n_dimers=nd, kinetics=KIN_SIMPLE,
+        exclusion=EXCL_PARTICLE, catalysis=CAT_DETERMINISTIC, rotation_sense=1,
+        mpc_every=int(round(deck["MPCt"] / deck["MDt"])), sort_every=int(deck["sort_step"]),
+        react_box_type=0, react_dir=0, cell_capacity=100, max_neighbour=30000, rattle_max_iter=100000,
+        init_plane=0, pad0=0, n_solvent=nt, seed=int(deck["seed"]), init_count=[na0, nb0, 0, 0],
+        mass=[deck["Ma"], deck["Mb"], 1.0, 1.0], eps_c=[deck["EaC"], deck["EbC"], 0.0, 0.0],
+        eps_n=[deck["EaN"], deck["EbN"], 0.0, 0.0], rc=deck["Rc"], rn=deck["Rn"], dcn=deck["Dcn"],
+        mc=mc, mn=mn, rw=1.0, ew=0.0, rm_delta=0.0, em=0.0, rp_ab=deck["RPab"], rp_ba=deck["RPba"],
+        kT=deck["T"], skin=deck["skinrad"], rot_angle=deck["rotang"], md_dt=deck["MDt"], mpc_dt=deck["MPCt"],
+        k=[deck["k1"], 0, 0, 0, 0, 0], precision=PREC_FP32, shell_capacity=0,
+        variant=VARIANT_ROTOR, layout=layout, layout_rows=rows, layout_cols=cols, reserved=[0] * 2,
+        tether_k=deck["k_harm"], tether_z=deck["Rc"] + deck["gap"], layout_sep=sep,
     )
     cfg.update(kw)
     return cfg
@@ -185,7 +247,7 @@ def selkov_config(deck, **kw):
         rp_ab=deck["RPfg"], rp_ba=deck["RPgf"], kT=deck["T"] / 5.0, skin=1.5, rot_angle=math.pi / 2,
         md_dt=deck["MDt"], mpc_dt=deck["MPCt"],
         k=[deck["k1"], deck["k2"], deck["k3"], deck["k4"], deck["k5"], deck["k6"]],
-        precision=PREC_FP32, shell_capacity=0, reserved=[0] * 6,
+        precision=PREC_FP32, shell_capacity=0, reserved=[0] * 2,
     )
     cfg.update(kw)
     return cfg
@@ -218,6 +280,27 @@ def workload(name, scale=1.0, **kw):
                     cell_capacity=200, n_solvent=n, init_count=[nf, ng, 0, n - nf - ng],
                     eps_c=[1.0, 1.0, 0.0, 1.0], eps_n=[1.0, 0.1, 0.0, 1.0],
                     k=[1.0, 0.1, 1.0, 0.0, 0.01, 0.0], sort_every=10000)
+    elif name in ("rot", "rot_line"):
+        # rotors of rotational_code/2d_array (a grid) or linear_periodic_ci (a
+        # line) with their input decks' parameters, scaled with the box
+        lx = max(16, int(round((64 if name == "rot" else 256) * scale)))
+        ly = max(16, int(round(64 * scale)))
+        lz = max(8, int(round(32 * scale)))
+        rc = rn = 2.0
+        dcn = 5.0
+        pitch = dcn + 2.0 * rc * 2.0 ** (1.0 / 6.0)
+        common = dict(lx=lx, ly=ly, lz=lz, geometry=GEOM_WALLS, kinetics=KIN_SIMPLE, react_box_type=0,
+                      rc=rc, rn=rn, dcn=dcn, eps_c=[1.0 if name == "rot_line" else 0.1, 1.0 if name == "rot_line"
+                                                    else 0.1, 0.0, 0.0],
+                      eps_n=[0.1, 1.0, 0.0, 0.0], rw=1.0, ew=0.0, rm_delta=0.0, em=0.0, kT=0.2, skin=0.7,
+                      rot_angle=math.pi / 2, md_dt=0.005, mpc_dt=0.1, k=[0.001, 0, 0, 0, 0, 0],
+                      variant=VARIANT_ROTOR, tether_k=1000.0, tether_z=rc + 1.0)
+        if name == "rot":
+            n = max(1, min(6, int(lx // pitch), int(ly // pitch)))
+            args = dict(common, n_dimers=n * n, layout=LAYOUT_GRID, layout_rows=n, layout_cols=n, layout_sep=0.0)
+        else:
+            nd = max(1, int(lx // pitch) // 2)
+            args = dict(common, n_dimers=nd, layout=LAYOUT_LINE, layout_sep=(lx - nd * pitch) / nd)
     else:
         raise ValueError("unknown workload %r" % name)
     if "n_solvent" in kw and "init_count" not in kw and name == "c2":

@@ -137,6 +137,8 @@ struct KParams {
   double mot_cut2[3], mot_R6[3], mot_R12[3], mot_r6R6[3], mot_r12R12[3];
   float mot_cut2f[3];
   double em, ew, rwc, rwn;
+  int rotor;             // anchored dimers, harmonic z tether, no motor-motor LJ
+  double tether_k, tether_z;
   double mc, mn, dcn;
   // dimer constants, computed once on the host with the kernel's expressions
   double hIMc, hIMn, IIM;          // (dt/2)/Mc, (dt/2)/Mn, 1/(1/Mc + 1/Mn)

@@ -123,6 +123,8 @@ struct EngineBase {
   virtual int download(double* x, double* y, double* z, double* vx, double* vy, double* vz, int32_t* flag,
                        double* dpos, double* dvel, double* dforce) = 0;
   virtual int set_order(const int32_t* order, int64_t n) = 0;
+  virtual int set_anchors(const double* a) = 0;
+  virtual int get_anchors(double* a) = 0;
   virtual int set_step(int64_t cstep, int32_t tc) = 0;
   virtual int initial() = 0;
   virtual int prepare() = 0;
@@ -276,6 +278,12 @@ struct Engine : EngineBase {
       return MPCMD_ERR_CONFIG;
     if (c.mpc_every <= 0 || c.md_dt <= 0 || c.cell_capacity <= 0 || c.cell_capacity > 255) return MPCMD_ERR_CONFIG;
     if (c.kinetics == MPCMD_KIN_SELKOV && c.geometry != MPCMD_GEOM_PERIODIC) return MPCMD_ERR_CONFIG;
+    if (c.variant != MPCMD_VARIANT_MOTOR && c.variant != MPCMD_VARIANT_ROTOR) return MPCMD_ERR_CONFIG;
+    if (c.variant == MPCMD_VARIANT_ROTOR && !(c.tether_k >= 0.0)) return MPCMD_ERR_CONFIG;
+    if (c.layout == MPCMD_LAYOUT_GRID ? (c.layout_rows <= 0 || c.layout_cols <= 0 ||
+                                         (int64_t)c.layout_rows * c.layout_cols != c.n_dimers)
+                                      : (c.layout != MPCMD_LAYOUT_RANDOM && c.layout != MPCMD_LAYOUT_LINE))
+      return MPCMD_ERR_CONFIG;
     int dev = 0;
     CK(cudaGetDevice(&dev));
     int nsm = 0;
@@ -346,6 +354,8 @@ struct Engine : EngineBase {
       kp.mot_R6[t] = R6; kp.mot_R12[t] = R12; kp.mot_r6R6[t] = 6.0 * R6; kp.mot_r12R12[t] = 12.0 * R12;
     }
     kp.em = c.em; kp.ew = c.ew; kp.rwc = c.rw + c.rc; kp.rwn = c.rw + c.rn;
+    kp.rotor = c.variant == MPCMD_VARIANT_ROTOR ? 1 : 0;
+    kp.tether_k = c.tether_k; kp.tether_z = c.tether_z;
     kp.mc = c.mc; kp.mn = c.mn; kp.dcn = c.dcn;
     kp.hIMc = (0.5 * c.md_dt) / c.mc; kp.hIMn = (0.5 * c.md_dt) / c.mn;
     kp.IIM = 1.0 / ((1.0 / c.mc) + (1.0 / c.mn));
@@ -375,6 +385,7 @@ struct Engine : EngineBase {
     const int64_t ns1 = std::max<int64_t>(ns, 1), nd1 = std::max<int64_t>(c.n_dimers, 1);
     r |= alloc(d.dpos, 3 * ns1); r |= alloc(d.dvel, 3 * ns1); r |= alloc(d.dfrc, 3 * ns1); r |= alloc(d.dq, 3 * ns1);
     r |= alloc(d.srel, ns1); r |= alloc(d.facc, 4 * ns1); r |= alloc(d.fmot, 4 * ns1); r |= alloc(d.dpot, nd1);
+    r |= alloc(d.anchor, 3 * nd1);
     int64_t nbins = (int64_t)kp.nbx * kp.nby * kp.nbz;
     r |= alloc(d.bin_cnt, nbins); r |= alloc(d.bin_list, nbins * BIN_SLOTS);
     r |= alloc(d.bin_mask, (nbins + 31) / 32);
@@ -400,6 +411,7 @@ struct Engine : EngineBase {
     CK(cudaMemsetAsync(d.facc, 0, sizeof(double) * 4 * std::max<int64_t>(ns, 1), st));
     CK(cudaMemsetAsync(d.fmot, 0, sizeof(double) * 4 * std::max<int64_t>(ns, 1), st));
     CK(cudaMemsetAsync(d.dq, 0, sizeof(double) * 3 * std::max<int64_t>(ns, 1), st));
+    CK(cudaMemsetAsync(d.anchor, 0, sizeof(double) * 3 * (size_t)nd1, st));
     CK(cudaMemsetAsync(d.p.flag, 0, (size_t)n, st));
     react = reactive_table(c);
     CK(cudaMemcpyAsync(d.react_box, react.data(), react.size(), cudaMemcpyHostToDevice, st));
@@ -497,6 +509,8 @@ struct Engine : EngineBase {
       if (dforce) CK(cudaMemcpyAsync(d.dfrc, dforce, nb, cudaMemcpyHostToDevice, st));
       else CK(cudaMemsetAsync(d.dfrc, 0, nb, st));
       Launch<T>::update_srel(d, kp, st);
+      int r = set_anchors(midpoints(dpos).data());
+      if (r) return r;
     }
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
     CK(cudaStreamSynchronize(st));
@@ -504,8 +518,39 @@ struct Engine : EngineBase {
     return MPCMD_OK;
   }
 
+  // motorCM(k,:) = 0.5 * (X(k,1) + X(k,2)) (rotational_code/2d_array/initial_mod.f95:86-88)
+  std::vector<double> midpoints(const double* pos) const {
+    std::vector<double> m(3 * (size_t)kp.nd);
+    for (int k = 0; k < kp.nd; ++k)
+      for (int q = 0; q < 3; ++q) m[3 * k + q] = 0.5 * (pos[3 * (2 * k) + q] + pos[3 * (2 * k + 1) + q]);
+    return m;
+  }
+
+  int set_anchors(const double* a) override {
+    if (kp.nd == 0) return MPCMD_OK;
+    if (!a) return MPCMD_ERR_CONFIG;
+    CK(cudaMemcpyAsync(d.anchor, a, sizeof(double) * 3 * (size_t)kp.nd, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return MPCMD_OK;
+  }
+
+  int get_anchors(double* a) override {
+    if (kp.nd == 0) return MPCMD_OK;
+    if (!a) return MPCMD_ERR_CONFIG;
+    CK(cudaMemcpyAsync(a, d.anchor, sizeof(double) * 3 * (size_t)kp.nd, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return MPCMD_OK;
+  }
+
   int download(double* x, double* y, double* z, double* vx, double* vy, double* vz, int32_t* flag,
                double* dpos, double* dvel, double* dforce) override {
+    return download_state(x, y, z, vx, vy, vz, flag, dpos, dvel, dforce, false);
+  }
+
+  // `current`: every particle at the current step (a checkpoint) instead of
+  // the reference's view with the outside particles at the last rebuild
+  int download_state(double* x, double* y, double* z, double* vx, double* vy, double* vz, int32_t* flag,
+                     double* dpos, double* dvel, double* dforce, bool current) {
     if (advanced) return MPCMD_ERR_STATE;
     flush_shell();
     // component c is converted into buffer c & 1 on st while component c - 1
@@ -520,7 +565,8 @@ struct Engine : EngineBase {
       if (!outs[c]) continue;
       const int b = k++ & 1;
       CK(cudaStreamWaitEvent(st, copied[b], 0));
-      Launch<T>::download_convert(d, kp, buf[b], c, time_count, (int)(last_rebuild - last_full), st);
+      Launch<T>::download_convert(d, kp, buf[b], c, time_count, (int)(last_rebuild - last_full), current ? 1 : 0,
+                                  st);
       CK(cudaEventRecord(done[b], st));
       CK(cudaStreamWaitEvent(cst, done[b], 0));
       CK(cudaMemcpyAsync(outs[c], buf[b], sizeof(double) * kp.n, cudaMemcpyDeviceToHost, cst));
@@ -624,6 +670,17 @@ struct Engine : EngineBase {
 
   int prepare() override {
     // main_pattern.f95:168-187 (the reactive grid table is built at create)
+    if (advanced) return MPCMD_ERR_STATE;
+    if (prepared) {
+      // a context that has stepped since its state was set: a full list pass
+      // streams the lazily moved outside particles to this step and the flush
+      // writes the shell members back, so the run restarts from the state of
+      // this step
+      regather_shell();
+      int r = do_rebuild(cstep, time_count, false);
+      if (r) return r < 0 ? MPCMD_ERR_STATE : r;
+      flush_shell();
+    }
     home_shell = false;
     watch_valid = false;
     advanced = false;
@@ -643,6 +700,10 @@ struct Engine : EngineBase {
     if (r) return r;
     if (h.status) return dev_status_to_api(h.status);
     if (kp.ns == 0) std::swap(d.sh, d.sh2);   // (with spheres sort_shell filled d.sh)
+    // the first half kick of the run uses zero pair forces, as after
+    // initial_mod.f95 (FpairX = 0)
+    CK(cudaMemsetAsync(d.sh.pf, 0, sizeof(T) * 3 * PAIRMAX * (size_t)d.sh.cap, st));
+    CK(cudaStreamSynchronize(st));
     n_inside = h.n_inside;
     time_penetrate = h.time_penetrate;
     time_count = 0;
@@ -829,7 +890,34 @@ struct Engine : EngineBase {
       else if (dd < -0.5 * Lq) dd += Lq;
       return dd;
     };
-    for (int i = 0; i < cfg.n_dimers; ++i) {
+    if (cfg.layout != MPCMD_LAYOUT_RANDOM) {
+      // rotational_code/2d_array/initial_mod.f95:68-90 (grid, row-major over
+      // numrows x numcols) and linear_periodic_ci/initial_mod.f95:72-88 (line
+      // along x): motor centres at the pitch Dcn + 2 Rc 2^(1/6) + sep in the
+      // plane z = zdimeq, each with a uniform in-plane orientation
+      const bool grid = cfg.layout == MPCMD_LAYOUT_GRID;
+      const double sep = cfg.layout_sep, rows = cfg.layout_rows, cols = cfg.layout_cols;
+      for (int i = 0; i < cfg.n_dimers; ++i) {
+        double theta, unused;
+        contract_pair(cfg.seed, TAG_INIT_DIMER, (uint32_t)i, 0, 0, theta, unused);
+        theta = 2. * kPi * theta;
+        const double w = dcn + 2. * rc * cut;
+        double cx, cy;
+        if (grid) {
+          const int64_t j = i / cfg.layout_cols + 1, k = i % cfg.layout_cols + 1;
+          cx = 0.5 * (L[0] - w * cols - sep * (cols - 1)) + 0.5 * w + (double)(k - 1) * (w + sep);
+          cy = 0.5 * (L[1] - (w + sep) * (rows - 1) - w) + 0.5 * w + (double)(j - 1) * (w + sep);
+        } else {
+          cx = 0.5 * sep + 0.5 * w + (double)i * (w + sep);
+          cy = L[1] * 0.5;
+        }
+        double* X1 = &pos[3 * (2 * i)];
+        double* X2 = &pos[3 * (2 * i + 1)];
+        X1[0] = cx + 0.5 * dcn * std::cos(theta); X1[1] = cy + 0.5 * dcn * std::sin(theta); X1[2] = cfg.tether_z;
+        X2[0] = cx - 0.5 * dcn * std::cos(theta); X2[1] = cy - 0.5 * dcn * std::sin(theta); X2[2] = cfg.tether_z;
+      }
+    }
+    for (int i = 0; i < cfg.n_dimers && cfg.layout == MPCMD_LAYOUT_RANDOM; ++i) {
       int64_t at;
       for (at = 0; at < 100000000; ++at) {
         double ux, uy, uz, uphi, uth, unused;
@@ -881,6 +969,8 @@ struct Engine : EngineBase {
       CK(cudaMemsetAsync(d.dvel, 0, nb, st));
       CK(cudaMemsetAsync(d.dfrc, 0, nb, st));
       Launch<T>::update_srel(d, kp, st);
+      int r = set_anchors(midpoints(pos.data()).data());
+      if (r) return r;
     }
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
     Launch<T>::build_bins(d, kp, 0, st);
@@ -1164,7 +1254,11 @@ struct Engine : EngineBase {
 // Device-state snapshot (the role of restart_mod.f95 / Restart.f90 plus the
 // RNG position, which for counter-based streams is the step counter).  The
 // file is written to <path>.tmp and renamed, so an interrupted write keeps the
-// previous checkpoint; a checksum guards the payload.
+// previous checkpoint; a checksum guards the payload.  Version 2 files hold
+// every particle at the checkpoint step (the outside particles streamed over
+// their pending lag, time_count 0) and the rotor anchors, so a restored and
+// prepared context goes on as the original one does after mpcmd_prepare;
+// version 1 files (the reference's view, the lag in time_count) still load.
 struct CkptHeader {
   char magic[8];
   int32_t version, precision;
@@ -1186,22 +1280,28 @@ int Engine<T>::checkpoint(const char* path) {
   const int64_t n = kp.n, ns = kp.ns;
   std::vector<double> buf((size_t)(6 * n + 9 * ns));
   std::vector<int32_t> fl((size_t)n);
-  int r = download(buf.data(), buf.data() + n, buf.data() + 2 * n, buf.data() + 3 * n, buf.data() + 4 * n,
-                   buf.data() + 5 * n, fl.data(), buf.data() + 6 * n, buf.data() + 6 * n + 3 * ns,
-                   buf.data() + 6 * n + 6 * ns);
+  // version 2: every particle at the current step (time_count 0 on restore)
+  int r = download_state(buf.data(), buf.data() + n, buf.data() + 2 * n, buf.data() + 3 * n, buf.data() + 4 * n,
+                         buf.data() + 5 * n, fl.data(), buf.data() + 6 * n, buf.data() + 6 * n + 3 * ns,
+                         buf.data() + 6 * n + 6 * ns, true);
+  if (r) return r;
+  std::vector<double> anc(3 * (size_t)kp.nd);
+  r = get_anchors(anc.data());
   if (r) return r;
   CkptHeader h{};
   std::memcpy(h.magic, "MPCMDCK1", 8);
-  h.version = 1; h.precision = (int32_t)(sizeof(T) * 8);
-  h.n = n; h.ns = ns; h.cstep = cstep; h.time_count = time_count;
+  h.version = 2; h.precision = (int32_t)(sizeof(T) * 8);
+  h.n = n; h.ns = ns; h.cstep = cstep; h.time_count = 0;
   h.lx = kp.lx; h.ly = kp.ly; h.lz = kp.lz; h.seed = cfg.seed;
   uint64_t cs = fnv1a(buf.data(), buf.size() * 8, 1469598103934665603ull);
-  h.checksum = fnv1a(fl.data(), fl.size() * 4, cs);
+  cs = fnv1a(fl.data(), fl.size() * 4, cs);
+  h.checksum = fnv1a(anc.data(), anc.size() * 8, cs);
   std::string tmp = std::string(path) + ".tmp";
   FILE* f = std::fopen(tmp.c_str(), "wb");
   if (!f) return MPCMD_ERR_IO;
   bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(buf.data(), 8, buf.size(), f) == buf.size() &&
-            std::fwrite(fl.data(), 4, fl.size(), f) == fl.size();
+            std::fwrite(fl.data(), 4, fl.size(), f) == fl.size() &&
+            std::fwrite(anc.data(), 8, anc.size(), f) == anc.size();
   ok = (std::fclose(f) == 0) && ok;
   if (!ok || std::rename(tmp.c_str(), path) != 0) { std::remove(tmp.c_str()); return MPCMD_ERR_IO; }
   return MPCMD_OK;
@@ -1213,22 +1313,28 @@ int Engine<T>::restore(const char* path) {
   if (!f) return MPCMD_ERR_IO;
   CkptHeader h{};
   if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, "MPCMDCK1", 8) != 0 || h.n != kp.n ||
-      h.ns != kp.ns || h.lx != kp.lx || h.ly != kp.ly || h.lz != kp.lz) {
+      h.ns != kp.ns || h.lx != kp.lx || h.ly != kp.ly || h.lz != kp.lz || h.version < 1 || h.version > 2) {
     std::fclose(f);
     return MPCMD_ERR_CHECKPOINT;
   }
   const int64_t n = kp.n, ns = kp.ns;
   std::vector<double> buf((size_t)(6 * n + 9 * ns));
   std::vector<int32_t> fl((size_t)n);
-  bool ok = std::fread(buf.data(), 8, buf.size(), f) == buf.size() && std::fread(fl.data(), 4, fl.size(), f) == fl.size();
+  // version 1 files end with the flags; version 2 adds the rotor anchors
+  std::vector<double> anc(h.version >= 2 ? 3 * (size_t)kp.nd : 0);
+  bool ok = std::fread(buf.data(), 8, buf.size(), f) == buf.size() && std::fread(fl.data(), 4, fl.size(), f) == fl.size() &&
+            std::fread(anc.data(), 8, anc.size(), f) == anc.size();
   std::fclose(f);
   if (!ok) return MPCMD_ERR_CHECKPOINT;
   uint64_t cs = fnv1a(buf.data(), buf.size() * 8, 1469598103934665603ull);
-  if (fnv1a(fl.data(), fl.size() * 4, cs) != h.checksum) return MPCMD_ERR_CHECKPOINT;
+  cs = fnv1a(fl.data(), fl.size() * 4, cs);
+  if (h.version >= 2) cs = fnv1a(anc.data(), anc.size() * 8, cs);
+  if (cs != h.checksum) return MPCMD_ERR_CHECKPOINT;
   int r = upload(buf.data(), buf.data() + n, buf.data() + 2 * n, buf.data() + 3 * n, buf.data() + 4 * n,
                  buf.data() + 5 * n, fl.data(), buf.data() + 6 * n, buf.data() + 6 * n + 3 * ns,
                  buf.data() + 6 * n + 6 * ns);
   if (r) return r;
+  if (h.version >= 2 && (r = set_anchors(anc.data()))) return r;
   cstep = h.cstep;
   time_count = h.time_count;
   last_rebuild = cstep - time_count;
@@ -1313,6 +1419,16 @@ int mpcmd_set_cell_order(mpcmd_ctx* ctx, const int32_t* order, int64_t n) {
   CTX_OK(ctx);
   if (!order) return MPCMD_ERR_CONFIG;
   return ctx->e->set_order(order, n);
+}
+
+int mpcmd_set_anchors(mpcmd_ctx* ctx, const double* anchors) {
+  CTX_OK(ctx);
+  return ctx->e->set_anchors(anchors);
+}
+
+int mpcmd_get_anchors(mpcmd_ctx* ctx, double* anchors) {
+  CTX_OK(ctx);
+  return ctx->e->get_anchors(anchors);
 }
 
 int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count) {

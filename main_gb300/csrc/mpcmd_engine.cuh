@@ -101,6 +101,7 @@ struct Dev {
   SphereRel<T>* srel;      // [ns] sphere positions as cell + offset
   double* facc;            // [ns*4] -sum F_pair (xyz) and sum of pair potentials
   double* fmot;            // [ns*4] motor-motor force and potential (j < k part)
+  double* anchor;          // [nd*3] rotor anchors (motorCM)
   double* dpot;            // [nd] potential of each dimer at the last force evaluation
   uint32_t* bin_cnt;       // [nbins]
   uint32_t* bin_mask;      // [ceil(nbins / 32)] bit b set: bin b lists a sphere
@@ -160,7 +161,7 @@ struct Launch {
   static void upload_comp(const Dev<T>& d, const KParams<T>& kp, const double* src, int comp, cudaStream_t st);
   static void upload_flag(const Dev<T>& d, const KParams<T>& kp, const int32_t* src, cudaStream_t st);
   static void download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
-                               int tc_defer, cudaStream_t st);
+                               int tc_defer, int current, cudaStream_t st);
   static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st);
   static void update_srel(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   // tc_defer > 0: bins also reach every sphere that a deferred particle,

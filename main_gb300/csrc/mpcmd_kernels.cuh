@@ -244,9 +244,13 @@ void Launch<T>::upload_flag(const Dev<T>& d, const KParams<T>& kp, const int32_t
 // streaming).  A free-flight member (FLAG_PASSIVE) is streamed by the tc steps
 // since the last rebuild; a deferred outside state (written at the last full
 // pass) by the tc_defer steps from that pass to the last rebuild.
+// State of a component as the reference holds it (outside particles at the
+// last rebuild: passive members streamed by tc, deferred ones by tc_defer),
+// or with `current` every particle at the current step (outside particles
+// written at the last rebuild streamed by tc, deferred ones by tc_defer + tc).
 template <typename T>
 __global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_box, double* out, int comp, int tc,
-                           int tc_defer) {
+                           int tc_defer, int current) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
     uint32_t c = p.cell[i];
@@ -255,7 +259,8 @@ __global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_b
     const uint8_t f = p.flag[i];
     int lag = 0;
     if (f & FLAG_PASSIVE) lag = tc;
-    else if (!(f & (FLAG_INLIST | FLAG_FRESH | FLAG_HOME_SHELL))) lag = tc_defer;
+    else if (!(f & (FLAG_INLIST | FLAG_FRESH | FLAG_HOME_SHELL))) lag = current ? tc_defer + tc : tc_defer;
+    else if (current && !(f & (FLAG_INLIST | FLAG_HOME_SHELL))) lag = tc;
     if (lag > 0) {
       uint8_t ff = f;
       stream_one(kp, react_box, c, ox, oy, oz, vx, vy, vz, ff, true, lag);
@@ -271,8 +276,8 @@ __global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_b
 
 template <typename T>
 void Launch<T>::download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
-                                 int tc_defer, cudaStream_t st) {
-  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, comp, tc, tc_defer);
+                                 int tc_defer, int current, cudaStream_t st) {
+  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, comp, tc, tc_defer, current);
   LAUNCH_COUNT();
 }
 
@@ -970,7 +975,8 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
     const int s = w, ks = s >> 1, is = s & 1;
     const SphereRel<T> rs = d.srel[s];
     double fx = 0., fy = 0., fz = 0., pot = 0.;
-    for (int t = lane; t < kp.ns; t += 32) {
+    // (rotors have no motor-motor LJ: rotational_code/2d_array/evolve_mod.f95:515-531)
+    for (int t = lane; t < (kp.rotor ? 0 : kp.ns); t += 32) {
       int kt = t >> 1, it = t & 1;
       if (kt == ks) continue;
       const SphereRel<T> rt = d.srel[t];
@@ -1556,6 +1562,144 @@ __global__ void k_dimer(Dev<T> d, KParams<T> kp, StepArgs a, int mode, double w3
   if (iters) atomicAdd(&d.ctr->rattle_iters, iters);
 }
 
+// rotational_code/2d_array/forces_mod.f95:177-201: harmonic z tether.
+__device__ __forceinline__ void harmonic_tether(const double zdim, const double zdimeq, const double k_harm,
+                                                double& f, double& pot) {
+  const double zdiff = zdim - zdimeq;
+  f = -1. * k_harm * zdiff;
+  pot = 0.5 * k_harm * (zdiff * zdiff);
+}
+
+// One thread per anchored rotor (rotational_code/2d_array/evolve_mod.f95:
+// 533-557 totals with the tether, :596-650 RATTLE velocities, :283-391
+// RATTLE positions), in the reference's FP64 operation sequence in both
+// builds (a handful of rotors per run).  Besides the bond, the positions hold
+// the midpoint 0.5 (X1 + X2) (wrapped into the box in x and y) at the anchor,
+// with the correction H = -4 IIM (midpoint - anchor) applied as H / (2 M) to
+// each sphere, and the velocities hold the midpoint velocity at zero.
+template <typename T>
+__global__ void k_rotor(Dev<T> d, KParams<T> kp, StepArgs a, int mode, int rattle_max) {
+  if (d.ctr->abort_step) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kp.nd) return;
+  const double dt = kp.dtd, Mc = kp.mc, Mn = kp.mn, Dcn = kp.dcn;
+  const double hIMc = kp.hIMc, hIMn = kp.hIMn, IIM = kp.IIM;
+  const bool per = kp.geometry == 1;
+  const int nwrap = per ? 3 : 2;
+  const int s1 = 2 * k, s2 = 2 * k + 1;
+  double X1[3], X2[3], V1[3], V2[3], F1[3], F2[3], Q1[3], Q2[3], A[3];
+  for (int c = 0; c < 3; ++c) {
+    X1[c] = d.dpos[3 * s1 + c]; X2[c] = d.dpos[3 * s2 + c];
+    V1[c] = d.dvel[3 * s1 + c]; V2[c] = d.dvel[3 * s2 + c];
+    F1[c] = d.dfrc[3 * s1 + c]; F2[c] = d.dfrc[3 * s2 + c];
+    Q1[c] = d.dq[3 * s1 + c]; Q2[c] = d.dq[3 * s2 + c];
+    A[c] = d.anchor[3 * k + c];
+  }
+  unsigned long long iters = 0;
+  if (mode & 1) {
+    double pot = 0.;
+    for (int i = 0; i < 2; ++i) {
+      const int s = 2 * k + i;
+      double* F = i == 0 ? F1 : F2;
+      double fw = 0., pw = 0.;
+      harmonic_tether((i == 0 ? X1 : X2)[2], kp.tether_z, kp.tether_k, fw, pw);
+      F[0] = d.facc[4 * s + 0];
+      F[1] = d.facc[4 * s + 1];
+      F[2] = d.facc[4 * s + 2] + fw;
+      pot += d.facc[4 * s + 3] + pw;
+      d.facc[4 * s + 0] = 0.; d.facc[4 * s + 1] = 0.; d.facc[4 * s + 2] = 0.; d.facc[4 * s + 3] = 0.;
+    }
+    d.dpot[k] = pot;
+    for (int c = 0; c < 3; ++c) { V1[c] = Q1[c] + hIMc * F1[c]; V2[c] = Q2[c] + hIMn * F2[c]; }
+    int acc = 0;
+    for (;;) {
+      double dV[3], dd[3], Vm[3];
+      for (int c = 0; c < 3; ++c) { dV[c] = V1[c] - V2[c]; dd[c] = X1[c] - X2[c]; }
+      dd[0] = dmin_image(dd[0], kp.Ld[0]);
+      dd[1] = dmin_image(dd[1], kp.Ld[1]);
+      if (per) dd[2] = dmin_image(dd[2], kp.Ld[2]);
+      const double Con2diff = dV[0] * dd[0] + dV[1] * dd[1] + dV[2] * dd[2];
+      for (int c = 0; c < 3; ++c) Vm[c] = 0.5 * (V1[c] + V2[c]);
+      if (fabs(Con2diff) < 1.e-8 && fabs(Vm[0]) < 1.e-8 && fabs(Vm[1]) < 1.e-8 && fabs(Vm[2]) < 1.e-8) break;
+      if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      const double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
+      for (int c = 0; c < 3; ++c) {
+        const double P = -(4.0 * Vm[c] * IIM);
+        V1[c] = V1[c] + O * dd[c] / Mc + 0.5 * P / Mc;
+        V2[c] = V2[c] - O * dd[c] / Mn + 0.5 * P / Mn;
+      }
+      acc++;
+    }
+    iters += acc;
+    for (int c = 0; c < 3; ++c) {
+      d.dvel[3 * s1 + c] = V1[c]; d.dvel[3 * s2 + c] = V2[c];
+      d.dfrc[3 * s1 + c] = F1[c]; d.dfrc[3 * s2 + c] = F2[c];
+    }
+  }
+  if (mode & 2) {
+    double pr1[3], pr2[3], dP[3];
+    for (int c = 0; c < 3; ++c) { pr1[c] = X1[c]; pr2[c] = X2[c]; dP[c] = X1[c] - X2[c]; }
+    dP[0] = dmin_image(dP[0], kp.Ld[0]);
+    dP[1] = dmin_image(dP[1], kp.Ld[1]);
+    if (per) dP[2] = dmin_image(dP[2], kp.Ld[2]);
+    for (int c = 0; c < 3; ++c) { Q1[c] = V1[c] + hIMc * F1[c]; Q2[c] = V2[c] + hIMn * F2[c]; }
+    for (int c = 0; c < 3; ++c) { X1[c] = X1[c] + dt * Q1[c]; X2[c] = X2[c] + dt * Q2[c]; }
+    for (int c = 0; c < nwrap; ++c) {
+      X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+      X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+    }
+    int acc = 0;
+    for (;;) {
+      double dd[3], D[3];
+      for (int c = 0; c < 3; ++c) dd[c] = X1[c] - X2[c];
+      dd[0] = dmin_image(dd[0], kp.Ld[0]);
+      dd[1] = dmin_image(dd[1], kp.Ld[1]);
+      if (per) dd[2] = dmin_image(dd[2], kp.Ld[2]);
+      for (int c = 0; c < 3; ++c) {
+        double m = 0.5 * (X1[c] + X2[c]);
+        if (c < 2) {
+          if (m >= kp.Ld[c]) m = m - kp.Ld[c];
+          else if (m < 0.) m = m + kp.Ld[c];
+        }
+        D[c] = m - A[c];
+      }
+      const double Con1diff = (dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) - Dcn * Dcn;
+      if (fabs(Con1diff) < 1.e-6 && fabs(D[0]) < 1.e-6 && fabs(D[1]) < 1.e-6 && fabs(D[2]) < 1.e-6) break;
+      if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      const double G = -(0.25 * Con1diff * IIM / (dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2]));
+      double H[3];
+      for (int c = 0; c < 3; ++c) H[c] = -(4.0 * IIM * D[c]);
+      for (int c = 0; c < 3; ++c) {
+        X1[c] = pr1[c] + Q1[c] * dt + G * dP[c] / Mc + 0.5 * H[c] / Mc;
+        X2[c] = pr2[c] + Q2[c] * dt - G * dP[c] / Mn + 0.5 * H[c] / Mn;
+      }
+      for (int c = 0; c < 3; ++c) {
+        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+      }
+      for (int c = 0; c < 3; ++c) {
+        Q1[c] = Q1[c] + G * dP[c] / (Mc * dt) + 0.5 * H[c] / (Mc * dt);
+        Q2[c] = Q2[c] - G * dP[c] / (Mn * dt) + 0.5 * H[c] / (Mn * dt);
+      }
+      acc++;
+    }
+    iters += acc;
+    for (int c = 0; c < 3; ++c) {
+      d.dpos[3 * s1 + c] = X1[c]; d.dpos[3 * s2 + c] = X2[c];
+      d.dq[3 * s1 + c] = Q1[c]; d.dq[3 * s2 + c] = Q2[c];
+    }
+    for (int i = 0; i < 2; ++i) {
+      const double* X = i == 0 ? X1 : X2;
+      const double fx = floor(X[0]), fy = floor(X[1]), fz = floor(X[2]);
+      SphereRel<T> r;
+      r.cx = (int)fx; r.cy = (int)fy; r.cz = (int)fz;
+      r.ox = (T)(X[0] - fx); r.oy = (T)(X[1] - fy); r.oz = (T)(X[2] - fz);
+      d.srel[2 * k + i] = r;
+    }
+  }
+  if (iters) atomicAdd(&d.ctr->rattle_iters, iters);
+}
+
 // Sum over the four lanes of a dimer's group (mask: those lanes, which
 // always take the same branches); every lane gets the same bits (the
 // butterfly adds the same pairs in every lane).
@@ -1689,7 +1833,9 @@ template <typename T>
 void Launch<T>::dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode, double w3,
                       int rattle_max, cudaStream_t st) {
   if (kp.nd == 0) return;
-  if (sizeof(T) == 4) {
+  if (kp.rotor) {
+    k_rotor<T><<<(kp.nd + 63) / 64, 64, 0, st>>>(d, kp, a, mode, rattle_max);
+  } else if (sizeof(T) == 4) {
     // four lanes per dimer, one 32-lane block per eight dimers (spread over the SMs)
     const int threads = 4 * kp.nd;
     k_dimer_split<T><<<(threads + 31) / 32, 32, 0, st>>>(d, kp, a, mode, w3, rattle_max);

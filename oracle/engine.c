@@ -117,6 +117,7 @@ orc_t* orc_create(const orc_params* p) {
   o->msd = calloc(n, 8);
   o->dpos = calloc(3 * ns, 8); o->dvel = calloc(3 * ns, 8); o->dfrc = calloc(3 * ns, 8);
   o->q = calloc(3 * ns, 8);
+  o->anchor = calloc(3 * ns, 8);
   o->nbnum = calloc(ns, 8);
   o->nb = calloc(ns * o->maxnb, 8);
   o->fpair = calloc(ns * o->maxnb * 3, 8);
@@ -135,7 +136,7 @@ orc_t* orc_create(const orc_params* p) {
   o->spair = calloc(n * 2 * 3, 8);
   o->spot = calloc(n, 8);
   if (!o->x || !o->y || !o->z || !o->vx || !o->vy || !o->vz || !o->flag || !o->msd ||
-      !o->dpos || !o->dvel || !o->dfrc || !o->q || !o->nbnum || !o->nb || !o->fpair ||
+      !o->dpos || !o->dvel || !o->dfrc || !o->q || !o->anchor || !o->nbnum || !o->nb || !o->fpair ||
       !o->pot || !o->in_list || !o->out_list || !o->newcell || !o->cm || !o->axis ||
       !o->ccount || !o->dcount || !o->dfirst || !o->affected || !o->react_box ||
       !o->fsx || !o->fsy || !o->fsz || !o->pfx || !o->pfy || !o->pfz || !o->spair || !o->spot) {
@@ -150,7 +151,7 @@ orc_t* orc_create(const orc_params* p) {
 void orc_destroy(orc_t* o) {
   if (!o) return;
   free(o->x); free(o->y); free(o->z); free(o->vx); free(o->vy); free(o->vz);
-  free(o->flag); free(o->msd); free(o->dpos); free(o->dvel); free(o->dfrc); free(o->q);
+  free(o->flag); free(o->msd); free(o->dpos); free(o->dvel); free(o->dfrc); free(o->q); free(o->anchor);
   free(o->nbnum); free(o->nb); free(o->fpair); free(o->pot); free(o->in_list);
   free(o->out_list); free(o->newcell); free(o->cm); free(o->axis); free(o->ccount);
   free(o->dcount); free(o->dfirst); free(o->affected); free(o->react_box); free(o->order);
@@ -160,6 +161,14 @@ void orc_destroy(orc_t* o) {
 }
 
 int orc_status(const orc_t* o) { return o ? o->status : ORC_ERR_STATE; }
+
+/* motorCM(k,:) = 0.5 * (X(k,1) + X(k,2)) on the positions as stored
+ * (rotational_code/2d_array/initial_mod.f95:86-88). */
+static void set_midpoint_anchors(orc_t* o) {
+  for (int k = 0; k < o->nd; ++k)
+    for (int c = 0; c < 3; ++c)
+      o->anchor[3 * k + c] = 0.5 * (o->dpos[3 * (2 * k) + c] + o->dpos[3 * (2 * k + 1) + c]);
+}
 
 int orc_set_state(orc_t* o, const double* x, const double* y, const double* z,
                   const double* vx, const double* vy, const double* vz,
@@ -174,7 +183,18 @@ int orc_set_state(orc_t* o, const double* x, const double* y, const double* z,
     if (dvel) memcpy(o->dvel, dvel, 3 * o->ns * 8);
     if (dforce) memcpy(o->dfrc, dforce, 3 * o->ns * 8);
     else memset(o->dfrc, 0, 3 * o->ns * 8);
+    set_midpoint_anchors(o);
   }
+  return ORC_OK;
+}
+
+int orc_set_anchors(orc_t* o, const double* anchors) {
+  if (o->nd > 0) memcpy(o->anchor, anchors, 3 * (size_t)o->nd * 8);
+  return ORC_OK;
+}
+
+int orc_get_anchors(const orc_t* o, double* anchors) {
+  if (o->nd > 0) memcpy(anchors, o->anchor, 3 * (size_t)o->nd * 8);
   return ORC_OK;
 }
 
@@ -447,7 +467,36 @@ int orc_initial(orc_t* o) {
   const int mt = o->rng_mode == ORC_RNG_MT;
   const int64_t max_attempts = 100000000;
 
-  for (int i = 0; i < o->nd; ++i) {
+  if (o->p.layout != ORC_LAYOUT_RANDOM) {
+    /* rotational_code/2d_array/initial_mod.f95:68-90 (grid, row-major over
+     * numrows x numcols) and linear_periodic_ci/initial_mod.f95:72-88 (line
+     * along x): motor centres on a lattice of pitch Dcn + 2 Rc 2^(1/6) + sep
+     * in the plane z = zdimeq, each with a uniform in-plane orientation */
+    const int grid = o->p.layout == ORC_LAYOUT_GRID;
+    const double cutoff = pow(2.0, 1.0 / 6.0), sep = o->p.layout_sep;
+    const double rows = o->p.layout_rows, cols = o->p.layout_cols;
+    if (grid ? (o->p.layout_rows * o->p.layout_cols != o->nd) : o->p.layout != ORC_LAYOUT_LINE)
+      return o->status = ORC_ERR_CONFIG;
+    for (int i = 0; i < o->nd; ++i) {
+      double theta = orc_draw(o, ORC_TAG_INIT_DIMER, i, 0, 0, 0);
+      theta = 2. * pi * theta;
+      const double w = dcn + 2. * rc * cutoff;
+      double cx, cy;
+      if (grid) {
+        const int64_t j = i / o->p.layout_cols + 1, k = i % o->p.layout_cols + 1;
+        cx = 0.5 * (o->L[0] - w * cols - sep * (cols - 1)) + 0.5 * w + (double)(k - 1) * (w + sep);
+        cy = 0.5 * (o->L[1] - (w + sep) * (rows - 1) - w) + 0.5 * w + (double)(j - 1) * (w + sep);
+      } else {
+        cx = 0.5 * sep + 0.5 * w + (double)i * (w + sep);
+        cy = o->L[1] * 0.5;
+      }
+      double* X1 = o->dpos + 3 * (2 * i);
+      double* X2 = o->dpos + 3 * (2 * i + 1);
+      X1[0] = cx + 0.5 * dcn * cos(theta); X1[1] = cy + 0.5 * dcn * sin(theta); X1[2] = o->p.tether_z;
+      X2[0] = cx - 0.5 * dcn * cos(theta); X2[1] = cy - 0.5 * dcn * sin(theta); X2[2] = o->p.tether_z;
+    }
+  }
+  for (int i = 0; i < o->nd && o->p.layout == ORC_LAYOUT_RANDOM; ++i) {
     int64_t a;
     for (a = 0; a < max_attempts; ++a) {
       double ux = orc_draw(o, ORC_TAG_INIT_DIMER, i, (uint32_t)a, 0, 0);
@@ -532,6 +581,7 @@ int orc_initial(orc_t* o) {
   if (err) return o->status = ORC_ERR_INIT;
 
   for (int s = 0; s < 3 * o->ns; ++s) { o->dvel[s] = 0.; o->dfrc[s] = 0.; }
+  set_midpoint_anchors(o);
   double* vel[3] = {o->vx, o->vy, o->vz};
   double sum[3] = {0., 0., 0.};
   if (mt) {
@@ -758,6 +808,114 @@ static void rattle_positions(orc_t* o, int k) {
   }
 }
 
+/* rotational_code/2d_array/evolve_mod.f95:283-391: RATTLE positions of an
+ * anchored rotor.  Besides the bond, the midpoint 0.5 (X1 + X2) (wrapped
+ * into the box in x and y) is held at the anchor motorCM(k): each iteration
+ * adds the bond correction G dP / M and the anchor correction H / (2 M),
+ * H = -4 IIM (midpoint - anchor), and wraps all three coordinates. */
+static void rattle_positions_rotor(orc_t* o, int k) {
+  const double dt = o->p.md_dt, Mc = o->p.mc, Mn = o->p.mn, Dcn = o->p.dcn;
+  const double hIMc = (0.5 * dt) / Mc, hIMn = (0.5 * dt) / Mn;
+  const double IIM = 1.0 / ((1.0 / Mc) + (1.0 / Mn));
+  const int per = o->p.geometry == ORC_GEOM_PERIODIC;
+  const double* A = o->anchor + 3 * k;
+  double* X1 = o->dpos + 3 * (2 * k);
+  double* X2 = o->dpos + 3 * (2 * k + 1);
+  double* V1 = o->dvel + 3 * (2 * k);
+  double* V2 = o->dvel + 3 * (2 * k + 1);
+  double* F1 = o->dfrc + 3 * (2 * k);
+  double* F2 = o->dfrc + 3 * (2 * k + 1);
+  double* Q1 = o->q + 3 * (2 * k);
+  double* Q2 = o->q + 3 * (2 * k + 1);
+  double pr1[3], pr2[3], dP[3];
+  for (int c = 0; c < 3; ++c) { pr1[c] = X1[c]; pr2[c] = X2[c]; dP[c] = X1[c] - X2[c]; }
+  for (int c = 0; c < (per ? 3 : 2); ++c) dP[c] = pbc_d(dP[c], o->L[c]);
+  for (int c = 0; c < 3; ++c) { Q1[c] = V1[c] + hIMc * F1[c]; Q2[c] = V2[c] + hIMn * F2[c]; }
+  for (int c = 0; c < 3; ++c) { X1[c] = X1[c] + dt * Q1[c]; X2[c] = X2[c] + dt * Q2[c]; }
+  for (int c = 0; c < (per ? 3 : 2); ++c) {
+    X1[c] = wrap_floor(X1[c], o->L[c]);
+    X2[c] = wrap_floor(X2[c], o->L[c]);
+  }
+  int64_t acc = 0;
+  for (;;) {
+    double d[3], D[3];
+    for (int c = 0; c < 3; ++c) d[c] = X1[c] - X2[c];
+    for (int c = 0; c < (per ? 3 : 2); ++c) d[c] = pbc_d(d[c], o->L[c]);
+    for (int c = 0; c < 3; ++c) {
+      double m = 0.5 * (X1[c] + X2[c]);
+      if (c < 2) {
+        if (m >= o->L[c]) m = m - o->L[c];
+        else if (m < 0.) m = m + o->L[c];
+      }
+      D[c] = m - A[c];
+    }
+    double Con1diff = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) - Dcn * Dcn;
+    if ((fabs(Con1diff) < 1.e-6 && fabs(D[0]) < 1.e-6 && fabs(D[1]) < 1.e-6 && fabs(D[2]) < 1.e-6))
+      break;
+    if (acc == o->p.rattle_max_iter) { o->status = ORC_ERR_RATTLE; break; }
+    double G = -(0.25 * Con1diff * IIM / (d[0] * dP[0] + d[1] * dP[1] + d[2] * dP[2]));
+    double H[3];
+    for (int c = 0; c < 3; ++c) H[c] = -(4.0 * IIM * D[c]);
+    for (int c = 0; c < 3; ++c) {
+      X1[c] = pr1[c] + Q1[c] * dt + G * dP[c] / Mc + 0.5 * H[c] / Mc;
+      X2[c] = pr2[c] + Q2[c] * dt - G * dP[c] / Mn + 0.5 * H[c] / Mn;
+    }
+    for (int c = 0; c < 3; ++c) {
+      X1[c] = wrap_floor(X1[c], o->L[c]);
+      X2[c] = wrap_floor(X2[c], o->L[c]);
+    }
+    for (int c = 0; c < 3; ++c) {
+      Q1[c] = Q1[c] + G * dP[c] / (Mc * dt) + 0.5 * H[c] / (Mc * dt);
+      Q2[c] = Q2[c] - G * dP[c] / (Mn * dt) + 0.5 * H[c] / (Mn * dt);
+    }
+    acc++;
+  }
+}
+
+/* rotational_code/2d_array/evolve_mod.f95:596-650: RATTLE velocities of an
+ * anchored rotor: the bond constraint (without the factor 2 of the motor
+ * form) and a zero midpoint velocity, P = -4 IIM (V1 + V2) / 2. */
+static void rattle_velocities_rotor(orc_t* o, int k) {
+  const double dt = o->p.md_dt, Mc = o->p.mc, Mn = o->p.mn, Dcn = o->p.dcn;
+  const double hIMc = (0.5 * dt) / Mc, hIMn = (0.5 * dt) / Mn;
+  const double IIM = 1.0 / ((1.0 / Mc) + (1.0 / Mn));
+  const int per = o->p.geometry == ORC_GEOM_PERIODIC;
+  double* X1 = o->dpos + 3 * (2 * k);
+  double* X2 = o->dpos + 3 * (2 * k + 1);
+  double* V1 = o->dvel + 3 * (2 * k);
+  double* V2 = o->dvel + 3 * (2 * k + 1);
+  double* F1 = o->dfrc + 3 * (2 * k);
+  double* F2 = o->dfrc + 3 * (2 * k + 1);
+  double* Q1 = o->q + 3 * (2 * k);
+  double* Q2 = o->q + 3 * (2 * k + 1);
+  for (int c = 0; c < 3; ++c) { V1[c] = Q1[c] + hIMc * F1[c]; V2[c] = Q2[c] + hIMn * F2[c]; }
+  int64_t acc = 0;
+  for (;;) {
+    double dV[3], d[3], Vm[3];
+    for (int c = 0; c < 3; ++c) { dV[c] = V1[c] - V2[c]; d[c] = X1[c] - X2[c]; }
+    for (int c = 0; c < (per ? 3 : 2); ++c) d[c] = pbc_d(d[c], o->L[c]);
+    double Con2diff = dV[0] * d[0] + dV[1] * d[1] + dV[2] * d[2];
+    for (int c = 0; c < 3; ++c) Vm[c] = 0.5 * (V1[c] + V2[c]);
+    if (fabs(Con2diff) < 1.e-8 && fabs(Vm[0]) < 1.e-8 && fabs(Vm[1]) < 1.e-8 && fabs(Vm[2]) < 1.e-8) break;
+    if (acc == o->p.rattle_max_iter) { o->status = ORC_ERR_RATTLE; break; }
+    double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
+    double P[3];
+    for (int c = 0; c < 3; ++c) P[c] = -(4.0 * Vm[c] * IIM);
+    for (int c = 0; c < 3; ++c) {
+      V1[c] = V1[c] + O * d[c] / Mc + 0.5 * P[c] / Mc;
+      V2[c] = V2[c] - O * d[c] / Mn + 0.5 * P[c] / Mn;
+    }
+    acc++;
+  }
+}
+
+/* rotational_code/2d_array/forces_mod.f95:177-201: harmonic z tether. */
+void orc_harmonic_tether(double zdim, double zdimeq, double k_harm, double* f, double* pot) {
+  const double zdiff = zdim - zdimeq;
+  *f = -1. * k_harm * zdiff;
+  *pot = 0.5 * k_harm * (zdiff * zdiff);
+}
+
 /* evolve_mod.f95:679-724 for dimer k. */
 static void rattle_velocities(orc_t* o, int k) {
   const double dt = o->p.md_dt, Mc = o->p.mc, Mn = o->p.mn, Dcn = o->p.dcn;
@@ -820,7 +978,11 @@ static void evolve(orc_t* o) {
     o->msd[i] = o->msd[i] + (o->vx[i] * o->vx[i] + o->vy[i] * o->vy[i] + o->vz[i] * o->vz[i]) * (dt * dt);
   }
   /* RATTLE positions :320-417 */
-  for (int k = 0; k < o->nd; ++k) rattle_positions(o, k);
+  const int rotor = o->p.variant == ORC_VARIANT_ROTOR;
+  for (int k = 0; k < o->nd; ++k) {
+    if (rotor) rattle_positions_rotor(o, k);
+    else rattle_positions(o, k);
+  }
   /* zero sphere forces :424-455 */
   for (int j = 0; j < 3 * o->ns; ++j) o->dfrc[j] = 0.;
   o->tpot = 0.;
@@ -859,6 +1021,14 @@ static void evolve(orc_t* o) {
   for (int k = 0; k < o->nd; ++k) {
     lj_mot_sol(o, 2 * k);
     lj_mot_sol(o, 2 * k + 1);
+    /* the rotor variant has no motor-motor LJ and a harmonic tether in place
+     * of the wall (rotational_code/2d_array/evolve_mod.f95:515-531) */
+    if (rotor) {
+      orc_harmonic_tether(o->dpos[3 * (2 * k) + 2], o->p.tether_z, o->p.tether_k, &fwall[2 * k], &wpot[2 * k]);
+      orc_harmonic_tether(o->dpos[3 * (2 * k + 1) + 2], o->p.tether_z, o->p.tether_k, &fwall[2 * k + 1],
+                          &wpot[2 * k + 1]);
+      continue;
+    }
     for (int j = 0; j < o->nd; ++j) {
       if (j == k) continue;
       for (int i = 0; i < 2; ++i)
@@ -902,7 +1072,10 @@ static void evolve(orc_t* o) {
     }
   free(fmot); free(fmotpot); free(fwall); free(wpot);
   kick_lists(o);
-  for (int k = 0; k < o->nd; ++k) rattle_velocities(o, k);
+  for (int k = 0; k < o->nd; ++k) {
+    if (rotor) rattle_velocities_rotor(o, k);
+    else rattle_velocities(o, k);
+  }
 }
 
 /* ------------------------------------------------------------ distribute -- */

@@ -14,6 +14,7 @@ struct orc {
   double* msd;                /* max_solvent_dist                                  */
   double *dpos, *dvel, *dfrc; /* [ns*3]                                            */
   double* q;                  /* RATTLE q vectors [ns*3]                           */
+  double* anchor;             /* rotor anchors motorCM [nd*3]                      */
   int64_t maxnb;
   int64_t* nbnum;             /* [ns]                                              */
   int64_t* nb;                /* [ns*maxnb]                                        */
@@ -51,6 +52,7 @@ struct orc {
 double orc_draw(orc_t* o, uint32_t tag, uint32_t index, uint32_t extra, uint32_t step, int which);
 void orc_lj_consts(double r, double* R6, double* R12, double* r6R6, double* r12R12);
 void orc_lj_mot_wall(double Lz, double zdim, double Ew, double Rw_plus_R, double* fwallz, double* potential);
+void orc_harmonic_tether(double zdim, double zdimeq, double k_harm, double* f, double* pot);
 void orc_selkov_cell(const double k[6], double tau, int32_t nF, int32_t nG, int32_t nI,
                      double x1, double x2, int* channel);
 #endif

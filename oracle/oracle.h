@@ -30,6 +30,10 @@ enum { ORC_KIN_NONE = 0, ORC_KIN_SIMPLE = 1, ORC_KIN_SELKOV = 2 };
 enum { ORC_EXCL_PARTICLE = 0, ORC_EXCL_CELLS = 1 };
 enum { ORC_CAT_DETERMINISTIC = 0, ORC_CAT_PROBABILISTIC = 1 };
 enum { ORC_RNG_CONTRACT = 0, ORC_RNG_MT = 1 };
+/* rotational_code variants: ROTOR anchors every dimer's midpoint
+ * (rotational_code/2d_array); dimer layouts of the initial placement. */
+enum { ORC_VARIANT_MOTOR = 0, ORC_VARIANT_ROTOR = 1 };
+enum { ORC_LAYOUT_RANDOM = 0, ORC_LAYOUT_GRID = 1, ORC_LAYOUT_LINE = 2 };
 
 /* Random-stream tags of the counter-based contract RNG (shared with the GPU). */
 enum {
@@ -76,6 +80,14 @@ typedef struct orc_params {
   double rp_ab, rp_ba;       /* catalytic conversion probabilities                  */
   double kT, skin, rot_angle, md_dt, mpc_dt;
   double k[6];               /* bulk rate constants                                 */
+  int32_t engine_only[2];    /* (precision, shell_capacity of the engine config)    */
+  /* rotational_code variants (2d_array, linear_periodic_ci) */
+  int32_t variant;           /* ORC_VARIANT_*                                       */
+  int32_t layout;            /* ORC_LAYOUT_*: dimer placement of orc_initial        */
+  int32_t layout_rows, layout_cols;  /* numrows, numcols of the grid layout         */
+  int32_t reserved[2];
+  double tether_k, tether_z; /* k_harm and zdimeq of the harmonic z tether          */
+  double layout_sep;         /* sep: gap between neighbouring motors of a layout    */
 } orc_params;
 
 typedef struct orc_obs {
@@ -106,6 +118,10 @@ int orc_set_state(orc_t* o, const double* x, const double* y, const double* z,
 int orc_get_state(const orc_t* o, double* x, double* y, double* z,
                   double* vx, double* vy, double* vz, int32_t* flag,
                   double* dpos, double* dvel, double* dforce);
+/* Rotor anchors (motorCM) [n_dimers*3].  orc_set_state and orc_initial set
+ * them to the midpoints of the dimers they receive or place. */
+int orc_set_anchors(orc_t* o, const double* anchors);
+int orc_get_anchors(const orc_t* o, double* anchors);
 int orc_set_cell_order(orc_t* o, const int32_t* order, int64_t n);
 int orc_set_cstep(orc_t* o, int64_t cstep, int32_t time_count);
 

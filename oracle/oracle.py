@@ -24,6 +24,9 @@ PARAM_FIELDS = [
     ("rc", _D), ("rn", _D), ("dcn", _D), ("mc", _D), ("mn", _D), ("rw", _D), ("ew", _D),
     ("rm_delta", _D), ("em", _D), ("rp_ab", _D), ("rp_ba", _D), ("kT", _D), ("skin", _D),
     ("rot_angle", _D), ("md_dt", _D), ("mpc_dt", _D), ("k", _D * 6),
+    ("engine_only", _I32 * 2),
+    ("variant", _I32), ("layout", _I32), ("layout_rows", _I32), ("layout_cols", _I32),
+    ("reserved", _I32 * 2), ("tether_k", _D), ("tether_z", _D), ("layout_sep", _D),
 ]
 
 
@@ -62,6 +65,8 @@ def lib():
             "orc_set_rng": (C.c_int, [P, C.c_int, C.c_uint32]),
             "orc_set_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
             "orc_get_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
+            "orc_set_anchors": (C.c_int, [P, dp]),
+            "orc_get_anchors": (C.c_int, [P, dp]),
             "orc_set_cell_order": (C.c_int, [P, ip, C.c_int64]),
             "orc_set_cstep": (C.c_int, [P, C.c_int64, C.c_int32]),
             "orc_initial": (C.c_int, [P]), "orc_prepare": (C.c_int, [P]),
@@ -216,6 +221,17 @@ class Oracle:
             for k in ("dpos", "dvel", "dforce"):
                 out[k] = out[k][:0]
         return out
+
+    def set_anchors(self, anchors):
+        a = np.ascontiguousarray(anchors, dtype=np.float64).reshape(-1, 3)
+        if a.shape[0] != self.ns // 2:
+            raise ValueError("anchors: one row per dimer")
+        self._check(lib().orc_set_anchors(self.h, _ptr(a, C.c_double)), "set_anchors")
+
+    def get_anchors(self):
+        a = np.zeros((max(self.ns // 2, 1), 3))
+        lib().orc_get_anchors(self.h, _ptr(a, C.c_double))
+        return a[: self.ns // 2]
 
     def set_cell_order(self, order):
         a = np.ascontiguousarray(order, dtype=np.int32)

@@ -65,8 +65,11 @@ def test_config_layout_matches_header_and_oracle():
         assert offs[i] == getattr(config.MpcmdConfig, name).offset, name
     for j, (name, _) in enumerate(O.PARAM_FIELDS):
         assert offs[len(fields) + j] == getattr(O.OrcParams, name).offset, name
-        # the shared prefix of the two structs is identical
-        assert getattr(O.OrcParams, name).offset == getattr(config.MpcmdConfig, name).offset
+        # the two structs share their layout; the oracle's engine_only words
+        # sit where the engine config holds precision and shell_capacity
+        twin = "precision" if name == "engine_only" else name
+        assert getattr(O.OrcParams, name).offset == getattr(config.MpcmdConfig, twin).offset, name
+    assert C.sizeof(O.OrcParams) == C.sizeof(config.MpcmdConfig)
 
 
 def test_reference_decks_parse():

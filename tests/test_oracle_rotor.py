@@ -1,0 +1,157 @@
+"""The rotor variant of the oracle (rotational_code/2d_array and
+linear_periodic_ci) against known answers of the reference code (CPU):
+
+  * the grid and line layouts of the initial placement
+    (2d_array/initial_mod.f95:68-90, linear_periodic_ci/initial_mod.f95:72-88),
+    restated here in numpy from the same draws;
+  * RATTLE holds every rotor's midpoint at its anchor and the bond length to
+    the tolerances of 2d_array/evolve_mod.f95:99-105 and the midpoint velocity
+    to those of :116-122;
+  * the harmonic tether of forces_mod.f95:177-201 is the only force on an
+    isolated rotor's spheres besides the solvent (no motor-motor LJ, no 9-3
+    wall);
+  * the anchors survive set/get and follow the state exchange.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from main_gb300 import config
+from oracle import oracle as O
+
+TAG_INIT_DIMER = 5
+
+
+def rotor_cfg(name="rot", **kw):
+    return config.workload(name, scale=0.5 if name == "rot" else 0.25, **kw)
+
+
+def expected_layout(cfg):
+    """Sphere positions of the layout, restated from the reference formulas."""
+    cut = 2.0 ** (1.0 / 6.0)
+    nd = cfg["n_dimers"]
+    dcn, rc, sep = cfg["dcn"], cfg["rc"], cfg["layout_sep"]
+    w = dcn + 2.0 * rc * cut
+    out = np.zeros((2 * nd, 3))
+    for i in range(nd):
+        theta = 2.0 * math.pi * O.contract_u01(cfg["seed"], TAG_INIT_DIMER, i, 0, 0, 0)
+        if cfg["layout"] == config.LAYOUT_GRID:
+            rows, cols = cfg["layout_rows"], cfg["layout_cols"]
+            j, k = i // cols, i % cols
+            cx = 0.5 * (cfg["lx"] - w * cols - sep * (cols - 1)) + 0.5 * w + k * (w + sep)
+            cy = 0.5 * (cfg["ly"] - (w + sep) * (rows - 1) - w) + 0.5 * w + j * (w + sep)
+        else:
+            cx = 0.5 * sep + 0.5 * w + i * (w + sep)
+            cy = cfg["ly"] * 0.5
+        out[2 * i] = (cx + 0.5 * dcn * math.cos(theta), cy + 0.5 * dcn * math.sin(theta), cfg["tether_z"])
+        out[2 * i + 1] = (cx - 0.5 * dcn * math.cos(theta), cy - 0.5 * dcn * math.sin(theta), cfg["tether_z"])
+    return out
+
+
+@pytest.mark.parametrize("name", ["rot", "rot_line"])
+def test_layout_matches_reference_formulas(name):
+    cfg = rotor_cfg(name)
+    o = O.Oracle(cfg, threads=4)
+    o.initial()
+    st = o.get_state()
+    exp = expected_layout(cfg)
+    assert np.abs(st["dpos"] - exp).max() <= 1e-12
+    # anchors are the midpoints of the placed rotors, in the box plane z = zdimeq
+    mid = 0.5 * (st["dpos"][0::2] + st["dpos"][1::2])
+    assert np.array_equal(o.get_anchors(), mid)
+    assert np.all(mid[:, 2] == cfg["tether_z"])
+    # neighbouring motors are a pitch apart (sep = 0 for the grid workload)
+    pitch = cfg["dcn"] + 2.0 * cfg["rc"] * 2.0 ** (1.0 / 6.0) + cfg["layout_sep"]
+    assert abs((mid[1, 0] - mid[0, 0]) - pitch) <= 1e-12
+    # no solvent particle starts inside a sphere's LJ range
+    d = st["dpos"]
+    for s in range(d.shape[0]):
+        dx = st["x"] - d[s, 0]
+        dy = st["y"] - d[s, 1]
+        dx -= cfg["lx"] * np.round(dx / cfg["lx"])
+        dy -= cfg["ly"] * np.round(dy / cfg["ly"])
+        r2 = dx * dx + dy * dy + (st["z"] - d[s, 2]) ** 2
+        assert r2.min() >= (cfg["rc"] * 2.0 ** (1.0 / 6.0)) ** 2
+
+
+@pytest.mark.parametrize("name", ["rot", "rot_line"])
+def test_rattle_holds_anchor_bond_and_midpoint_velocity(name):
+    cfg = rotor_cfg(name)
+    o = O.Oracle(cfg, threads=4)
+    o.initial()
+    anchors = o.get_anchors().copy()
+    o.prepare()
+    o.run(3 * cfg["mpc_every"])
+    st = o.get_state()
+    d = st["dpos"].reshape(-1, 2, 3)
+    v = st["dvel"].reshape(-1, 2, 3)
+    mid = 0.5 * (d[:, 0] + d[:, 1])
+    assert np.abs(mid - anchors).max() < 1e-6
+    bond2 = ((d[:, 0] - d[:, 1]) ** 2).sum(axis=1)
+    assert np.abs(bond2 - cfg["dcn"] ** 2).max() < 1e-6
+    assert np.abs(0.5 * (v[:, 0] + v[:, 1])).max() < 1e-8
+    # the rotors turn (the solvent pushes them) and stay near the tether plane
+    assert np.abs(v).max() > 0.0
+    assert np.abs(d[:, :, 2] - cfg["tether_z"]).max() < 0.05
+    assert o.status() == 0
+
+
+def test_tether_and_no_motor_motor_forces():
+    # two rotors whose spheres overlap in LJ range: with the rotor variant the
+    # sphere forces are the solvent forces plus the tether only
+    cfg = rotor_cfg("rot_line", n_dimers=2, layout=config.LAYOUT_LINE, layout_sep=-3.0, em=1.0,
+                    n_solvent=4, init_count=[4, 0, 0, 0])
+    o = O.Oracle(cfg, threads=1)
+    st = {k: np.array([1.0, 2.0, 3.0, 4.0]) for k in ("x", "y")}
+    st["z"] = np.full(4, cfg["lz"] - 0.5)
+    for k in ("vx", "vy", "vz"):
+        st[k] = np.zeros(4)
+    st["flag"] = np.zeros(4, dtype=np.int32)
+    dz = 0.01
+    st["dpos"] = np.array([[20.0, 8.0, cfg["tether_z"] + dz], [25.0, 8.0, cfg["tether_z"] + dz],
+                           [27.0, 8.0, cfg["tether_z"] - dz], [32.0, 8.0, cfg["tether_z"] - dz]])
+    st["dvel"] = np.zeros((4, 3))
+    o.set_state(st)
+    o.prepare()
+    o.run(1)
+    got = o.get_state()
+    f = got["dforce"]
+    # the tether force -k (z - zeq) at the positions after the RATTLE step
+    dzs = got["dpos"][:, 2] - cfg["tether_z"]
+    assert np.allclose(f[:, 2], -cfg["tether_k"] * dzs, rtol=0, atol=1e-9)
+    # sphere 1 of rotor 0 and sphere 0 of rotor 1 are 2 apart: a motor-motor
+    # LJ force would be large; the rotor variant has none
+    assert np.abs(f[:, 0]).max() == 0.0 and np.abs(f[:, 1]).max() == 0.0
+
+
+def test_anchor_exchange():
+    cfg = rotor_cfg("rot")
+    o = O.Oracle(cfg, threads=2)
+    o.initial()
+    st = o.get_state()
+    st["dpos"] = st["dpos"] + np.array([0.25, -0.5, 0.0])
+    o.set_state(st)
+    mid = 0.5 * (st["dpos"][0::2] + st["dpos"][1::2])
+    assert np.array_equal(o.get_anchors(), mid)
+    new = mid + 0.125
+    o.set_anchors(new)
+    assert np.array_equal(o.get_anchors(), new)
+    with pytest.raises(ValueError):
+        o.set_anchors(new[:-1])
+
+
+def test_rotational_decks_parse():
+    ref = "/root/reference/rotational_code"
+    if not os.path.isdir(ref):
+        pytest.skip("reference tree not mounted")
+    g = config.rotational_config(config.read_rotational_input(os.path.join(ref, "2d_array", "input.txt")))
+    assert (g["lx"], g["ly"], g["lz"], g["n_dimers"], g["layout_rows"], g["layout_cols"]) == (64, 64, 32, 36, 6, 6)
+    assert g["tether_k"] == 1000.0 and g["tether_z"] == 3.0 and g["mpc_every"] == 20
+    assert g["n_solvent"] == math.floor(10.0 * 64 * 64 * 32)
+    line = config.read_rotational_input(os.path.join(ref, "linear_periodic_ci", "input.txt"), config.LAYOUT_LINE)
+    c = config.rotational_config(line, config.LAYOUT_LINE)
+    assert (c["lx"], c["n_dimers"], c["layout"]) == (256, 26, config.LAYOUT_LINE)
+    pitch = c["dcn"] + 2.0 * c["rc"] * 2.0 ** (1.0 / 6.0)
+    assert abs(c["layout_sep"] - (256 - 26 * pitch) / 26) < 1e-12
