@@ -62,7 +62,8 @@ module mpcmd_shim
     integer(c_int32_t) :: variant
     integer(c_int32_t) :: layout
     integer(c_int32_t) :: layout_rows, layout_cols
-    integer(c_int32_t) :: reserved(2)
+    integer(c_int32_t) :: owner_tags
+    integer(c_int32_t) :: reserved
     real(c_double) :: tether_k, tether_z
     real(c_double) :: layout_sep
   end type mpcmd_config
@@ -90,6 +91,7 @@ module mpcmd_shim
   public :: mpcmd_sort, mpcmd_rebuild_lists, mpcmd_distribute, mpcmd_mpc_rotation, mpcmd_reaction
   public :: mpcmd_observables, mpcmd_checkpoint, mpcmd_restore, mpcmd_set_cell_order
   public :: mpcmd_concentration, mpcmd_dimer_axes, mpcmd_set_anchors, mpcmd_get_anchors
+  public :: mpcmd_set_owner_tags, mpcmd_get_owner_tags
   public :: mpcmd_check
 
   interface
@@ -136,6 +138,17 @@ module mpcmd_shim
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: anchors(*)
+    end function
+    ! type_B of rotational_code/linear_periodic_no_ci (global_mod.f95:72), [NT]
+    integer(c_int) function mpcmd_set_owner_tags(ctx, type_b) bind(C, name="mpcmd_set_owner_tags")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), intent(in) :: type_b(*)
+    end function
+    integer(c_int) function mpcmd_get_owner_tags(ctx, type_b) bind(C, name="mpcmd_get_owner_tags")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), intent(out) :: type_b(*)
     end function
     integer(c_int) function mpcmd_set_cell_order(ctx, order, n) bind(C, name="mpcmd_set_cell_order")
       import :: c_int, c_ptr, c_int32_t, c_int64_t

@@ -95,7 +95,12 @@ typedef struct mpcmd_config {
                                 there is no motor-motor LJ                          */
   int32_t layout;            /* MPCMD_LAYOUT_*: dimer placement of mpcmd_initial     */
   int32_t layout_rows, layout_cols;  /* numrows, numcols of the grid layout          */
-  int32_t reserved[2];
+  int32_t owner_tags;        /* 1: type_B of linear_periodic_no_ci (forces_mod.f95:79-121):
+                                the C sphere of motor k makes every particle in its
+                                cutoff a B of motor k, and a B acts as A on the
+                                spheres of every other motor (deterministic catalysis,
+                                simple kinetics, no reactive floor)                  */
+  int32_t reserved;
   double tether_k, tether_z; /* k_harm, zdimeq (= Rc + gap)                          */
   double layout_sep;         /* sep: gap between neighbouring motors of a layout     */
 } mpcmd_config;
@@ -138,6 +143,14 @@ int mpcmd_set_cell_order(mpcmd_ctx* ctx, const int32_t* order, int64_t n);
  * mpcmd_restore sets the checkpointed ones. */
 int mpcmd_set_anchors(mpcmd_ctx* ctx, const double* anchors);
 int mpcmd_get_anchors(mpcmd_ctx* ctx, double* anchors);
+/* Owner tags type_B [n_solvent]: the 1-based motor number of the C sphere
+ * that made a B particle, 0 for none (linear_periodic_no_ci/global_mod.f95:72).
+ * mpcmd_initial and mpcmd_upload_state clear them; the tags follow the
+ * particles through the sort (sort_hilbert_mod.f95:75) and are cleared by the
+ * B -> A reaction (reaction_simple_mod.f95:55).  MPCMD_ERR_CONFIG without
+ * owner_tags. */
+int mpcmd_set_owner_tags(mpcmd_ctx* ctx, const int32_t* type_b);
+int mpcmd_get_owner_tags(mpcmd_ctx* ctx, int32_t* type_b);
 int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count);
 
 /* Reference call surface ----------------------------------------------- */

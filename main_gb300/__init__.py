@@ -62,6 +62,8 @@ SIGNATURES = {
     "mpcmd_upload_state": (C.c_int, [_P, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
     "mpcmd_download_state": (C.c_int, [_P, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
     "mpcmd_set_cell_order": (C.c_int, [_P, _ip, C.c_int64]),
+    "mpcmd_set_owner_tags": (C.c_int, [_P, _ip]),
+    "mpcmd_get_owner_tags": (C.c_int, [_P, _ip]),
     "mpcmd_set_anchors": (C.c_int, [_P, _dp]),
     "mpcmd_get_anchors": (C.c_int, [_P, _dp]),
     "mpcmd_set_step": (C.c_int, [_P, C.c_int64, C.c_int32]),
@@ -219,6 +221,18 @@ class Engine:
         a = np.zeros((max(self.ns // 2, 1), 3))
         self._c(lib().mpcmd_get_anchors(self.h, _ptr(a, C.c_double)), "get_anchors")
         return a[: self.ns // 2]
+
+    def set_owner_tags(self, tags):
+        """type_B owner tags (1-based motor numbers, 0 for none), one per particle."""
+        a = np.ascontiguousarray(tags, dtype=np.int32)
+        if a.size != self.n:
+            raise ValueError("owner tags: one per solvent particle")
+        self._c(lib().mpcmd_set_owner_tags(self.h, _ptr(a, C.c_int32)), "set_owner_tags")
+
+    def get_owner_tags(self):
+        a = np.zeros(self.n, dtype=np.int32)
+        self._c(lib().mpcmd_get_owner_tags(self.h, _ptr(a, C.c_int32)), "get_owner_tags")
+        return a
 
     def cell_order(self):
         a = np.zeros(self.ncell, dtype=np.int32)

@@ -32,7 +32,7 @@ FIELDS = [
     ("rot_angle", _D), ("md_dt", _D), ("mpc_dt", _D), ("k", _D * 6),
     ("precision", _I32), ("shell_capacity", _I32),
     ("variant", _I32), ("layout", _I32), ("layout_rows", _I32), ("layout_cols", _I32),
-    ("reserved", _I32 * 2), ("tether_k", _D), ("tether_z", _D), ("layout_sep", _D),
+    ("owner_tags", _I32), ("reserved", _I32), ("tether_k", _D), ("tether_z", _D), ("layout_sep", _D),
 ]
 
 GEOM_WALLS, GEOM_PERIODIC = 0, 1
@@ -82,7 +82,7 @@ def base_config(**kw):
         rp_ab=1.0, rp_ba=0.0, kT=1.0 / 6.0, skin=1.5, rot_angle=2.0 * math.pi / 3.0,
         md_dt=0.01, mpc_dt=0.5, k=[0.01, 0, 0, 0, 0, 0],
         precision=PREC_FP32, shell_capacity=0, variant=VARIANT_MOTOR, layout=LAYOUT_RANDOM, layout_rows=0,
-        layout_cols=0, reserved=[0] * 2, tether_k=0.0, tether_z=0.0, layout_sep=0.0,
+        layout_cols=0, owner_tags=0, reserved=0, tether_k=0.0, tether_z=0.0, layout_sep=0.0,
     )
     cfg.update(kw)
     return finish(cfg)
@@ -179,7 +179,7 @@ def collective_config(deck, **kw):
         rc=deck["Rc"], rn=deck["Rn"], dcn=deck["Dcn"], mc=mc, mn=mn, rw=deck["Rw"], ew=deck["Ew"],
         rm_delta=deck["Rm_delta"], em=deck["Em"], rp_ab=deck["RPab"], rp_ba=deck["RPba"], kT=deck["T"],
         skin=deck["skinrad"], rot_angle=deck["rotang"], md_dt=deck["MDt"], mpc_dt=deck["MPCt"],
-        k=[deck["k1"], 0, 0, 0, 0, 0], precision=PREC_FP32, shell_capacity=0, reserved=[0] * 2,
+        k=[deck["k1"], 0, 0, 0, 0, 0], precision=PREC_FP32, shell_capacity=0, reserved=0,
     )
     cfg.update(kw)
     return cfg
@@ -193,7 +193,8 @@ def rotational_config(deck, layout=LAYOUT_GRID, **kw):
     """rotational_code/2d_array/main_rotation.f95:53-110 (grid of rotors) or
     linear_periodic_ci/main_rotation.f95:51-108 (line of rotors, sep derived
     at :52): anchored dimers with a harmonic z tether over a walled box, no
-    motor-motor LJ, no reactive floor, reaction_simple with the rate k1."""
+    motor-motor LJ, no reactive floor, reaction_simple with the rate k1.
+    ``owner_tags=1`` gives linear_periodic_no_ci (type_B owner tags)."""
     box = [int(deck["box1"]), int(deck["box2"]), int(deck["box3"])]
     vol = box[0] * box[1] * box[2]
     cutoff = 2.0 ** (1.0 / 6.0)
@@ -222,7 +223,7 @@ def rotational_config(deck, layout=LAYOUT_GRID, **kw):
         mc=mc, mn=mn, rw=1.0, ew=0.0, rm_delta=0.0, em=0.0, rp_ab=deck["RPab"], rp_ba=deck["RPba"],
         kT=deck["T"], skin=deck["skinrad"], rot_angle=deck["rotang"], md_dt=deck["MDt"], mpc_dt=deck["MPCt"],
         k=[deck["k1"], 0, 0, 0, 0, 0], precision=PREC_FP32, shell_capacity=0,
-        variant=VARIANT_ROTOR, layout=layout, layout_rows=rows, layout_cols=cols, reserved=[0] * 2,
+        variant=VARIANT_ROTOR, layout=layout, layout_rows=rows, layout_cols=cols, owner_tags=0, reserved=0,
         tether_k=deck["k_harm"], tether_z=deck["Rc"] + deck["gap"], layout_sep=sep,
     )
     cfg.update(kw)
@@ -247,7 +248,7 @@ def selkov_config(deck, **kw):
         rp_ab=deck["RPfg"], rp_ba=deck["RPgf"], kT=deck["T"] / 5.0, skin=1.5, rot_angle=math.pi / 2,
         md_dt=deck["MDt"], mpc_dt=deck["MPCt"],
         k=[deck["k1"], deck["k2"], deck["k3"], deck["k4"], deck["k5"], deck["k6"]],
-        precision=PREC_FP32, shell_capacity=0, reserved=[0] * 2,
+        precision=PREC_FP32, shell_capacity=0, reserved=0,
     )
     cfg.update(kw)
     return cfg
@@ -280,7 +281,7 @@ def workload(name, scale=1.0, **kw):
                     cell_capacity=200, n_solvent=n, init_count=[nf, ng, 0, n - nf - ng],
                     eps_c=[1.0, 1.0, 0.0, 1.0], eps_n=[1.0, 0.1, 0.0, 1.0],
                     k=[1.0, 0.1, 1.0, 0.0, 0.01, 0.0], sort_every=10000)
-    elif name in ("rot", "rot_line"):
+    elif name in ("rot", "rot_line", "rot_owner"):
         # rotors of rotational_code/2d_array (a grid) or linear_periodic_ci (a
         # line) with their input decks' parameters, scaled with the box
         lx = max(16, int(round((64 if name == "rot" else 256) * scale)))
@@ -290,8 +291,7 @@ def workload(name, scale=1.0, **kw):
         dcn = 5.0
         pitch = dcn + 2.0 * rc * 2.0 ** (1.0 / 6.0)
         common = dict(lx=lx, ly=ly, lz=lz, geometry=GEOM_WALLS, kinetics=KIN_SIMPLE, react_box_type=0,
-                      rc=rc, rn=rn, dcn=dcn, eps_c=[1.0 if name == "rot_line" else 0.1, 1.0 if name == "rot_line"
-                                                    else 0.1, 0.0, 0.0],
+                      rc=rc, rn=rn, dcn=dcn, eps_c=[0.1, 0.1, 0.0, 0.0] if name == "rot" else [1.0, 1.0, 0.0, 0.0],
                       eps_n=[0.1, 1.0, 0.0, 0.0], rw=1.0, ew=0.0, rm_delta=0.0, em=0.0, kT=0.2, skin=0.7,
                       rot_angle=math.pi / 2, md_dt=0.005, mpc_dt=0.1, k=[0.001, 0, 0, 0, 0, 0],
                       variant=VARIANT_ROTOR, tether_k=1000.0, tether_z=rc + 1.0)
@@ -299,8 +299,11 @@ def workload(name, scale=1.0, **kw):
             n = max(1, min(6, int(lx // pitch), int(ly // pitch)))
             args = dict(common, n_dimers=n * n, layout=LAYOUT_GRID, layout_rows=n, layout_cols=n, layout_sep=0.0)
         else:
+            # rot_owner: the line of linear_periodic_no_ci, B particles tagged
+            # with the motor that made them
             nd = max(1, int(lx // pitch) // 2)
-            args = dict(common, n_dimers=nd, layout=LAYOUT_LINE, layout_sep=(lx - nd * pitch) / nd)
+            args = dict(common, n_dimers=nd, layout=LAYOUT_LINE, layout_sep=(lx - nd * pitch) / nd,
+                        owner_tags=1 if name == "rot_owner" else 0)
     else:
         raise ValueError("unknown workload %r" % name)
     if "n_solvent" in kw and "init_count" not in kw and name == "c2":

@@ -138,6 +138,7 @@ struct KParams {
   float mot_cut2f[3];
   double em, ew, rwc, rwn;
   int rotor;             // anchored dimers, harmonic z tether, no motor-motor LJ
+  int owner_tags;        // B particles tagged with the motor that made them (type_B)
   double tether_k, tether_z;
   double mc, mn, dcn;
   // dimer constants, computed once on the host with the kernel's expressions

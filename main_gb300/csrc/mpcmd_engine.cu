@@ -125,6 +125,8 @@ struct EngineBase {
   virtual int set_order(const int32_t* order, int64_t n) = 0;
   virtual int set_anchors(const double* a) = 0;
   virtual int get_anchors(double* a) = 0;
+  virtual int set_owner_tags(const int32_t* t) = 0;
+  virtual int get_owner_tags(int32_t* t) = 0;
   virtual int set_step(int64_t cstep, int32_t tc) = 0;
   virtual int initial() = 0;
   virtual int prepare() = 0;
@@ -280,6 +282,10 @@ struct Engine : EngineBase {
     if (c.kinetics == MPCMD_KIN_SELKOV && c.geometry != MPCMD_GEOM_PERIODIC) return MPCMD_ERR_CONFIG;
     if (c.variant != MPCMD_VARIANT_MOTOR && c.variant != MPCMD_VARIANT_ROTOR) return MPCMD_ERR_CONFIG;
     if (c.variant == MPCMD_VARIANT_ROTOR && !(c.tether_k >= 0.0)) return MPCMD_ERR_CONFIG;
+    if (c.owner_tags != 0 &&
+        (c.owner_tags != 1 || c.catalysis != MPCMD_CAT_DETERMINISTIC || c.kinetics == MPCMD_KIN_SELKOV ||
+         (c.geometry == MPCMD_GEOM_WALLS && c.react_box_type >= 1 && c.react_box_type <= 6)))
+      return MPCMD_ERR_CONFIG;
     if (c.layout == MPCMD_LAYOUT_GRID ? (c.layout_rows <= 0 || c.layout_cols <= 0 ||
                                          (int64_t)c.layout_rows * c.layout_cols != c.n_dimers)
                                       : (c.layout != MPCMD_LAYOUT_RANDOM && c.layout != MPCMD_LAYOUT_LINE))
@@ -355,6 +361,7 @@ struct Engine : EngineBase {
     }
     kp.em = c.em; kp.ew = c.ew; kp.rwc = c.rw + c.rc; kp.rwn = c.rw + c.rn;
     kp.rotor = c.variant == MPCMD_VARIANT_ROTOR ? 1 : 0;
+    kp.owner_tags = c.owner_tags;
     kp.tether_k = c.tether_k; kp.tether_z = c.tether_z;
     kp.mc = c.mc; kp.mn = c.mn; kp.dcn = c.dcn;
     kp.hIMc = (0.5 * c.md_dt) / c.mc; kp.hIMn = (0.5 * c.md_dt) / c.mn;
@@ -385,7 +392,6 @@ struct Engine : EngineBase {
     const int64_t ns1 = std::max<int64_t>(ns, 1), nd1 = std::max<int64_t>(c.n_dimers, 1);
     r |= alloc(d.dpos, 3 * ns1); r |= alloc(d.dvel, 3 * ns1); r |= alloc(d.dfrc, 3 * ns1); r |= alloc(d.dq, 3 * ns1);
     r |= alloc(d.srel, ns1); r |= alloc(d.facc, 4 * ns1); r |= alloc(d.fmot, 4 * ns1); r |= alloc(d.dpot, nd1);
-    r |= alloc(d.anchor, 3 * nd1);
     int64_t nbins = (int64_t)kp.nbx * kp.nby * kp.nbz;
     r |= alloc(d.bin_cnt, nbins); r |= alloc(d.bin_list, nbins * BIN_SLOTS);
     r |= alloc(d.bin_mask, (nbins + 31) / 32);
@@ -401,6 +407,9 @@ struct Engine : EngineBase {
     r |= alloc(d.scnt, cmax); r |= alloc(d.sstart, kp.ncell); r |= alloc(d.sfill, kp.ncell);
     r |= alloc(d.scan_tmp, scan_tmp_words(kp.ncell));
     r |= alloc(d.ctr, 1);
+    // (the variant arrays last: the allocations above keep their placement)
+    r |= alloc(d.anchor, 3 * nd1);
+    if (c.owner_tags) { r |= alloc(d.owner, n); r |= alloc(d.owner2, n); }
     if (r) return MPCMD_ERR_ALLOC;
 
     CK(cudaMemsetAsync(d.acc, 0, (sizeof(T) == 4 ? 16 : 32) * (size_t)kp.ncell_shift, st));
@@ -412,6 +421,7 @@ struct Engine : EngineBase {
     CK(cudaMemsetAsync(d.fmot, 0, sizeof(double) * 4 * std::max<int64_t>(ns, 1), st));
     CK(cudaMemsetAsync(d.dq, 0, sizeof(double) * 3 * std::max<int64_t>(ns, 1), st));
     CK(cudaMemsetAsync(d.anchor, 0, sizeof(double) * 3 * (size_t)nd1, st));
+    if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)n, st));
     CK(cudaMemsetAsync(d.p.flag, 0, (size_t)n, st));
     react = reactive_table(c);
     CK(cudaMemcpyAsync(d.react_box, react.data(), react.size(), cudaMemcpyHostToDevice, st));
@@ -498,6 +508,7 @@ struct Engine : EngineBase {
       Launch<T>::upload_comp(d, kp, buf[b], c, st);
       CK(cudaEventRecord(used[b], st));
     }
+    if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)kp.n, st));
     CK(cudaMemcpyAsync(d.staging_i, flag, sizeof(int32_t) * kp.n, cudaMemcpyHostToDevice, cst));
     CK(cudaEventRecord(copied[0], cst));
     CK(cudaStreamWaitEvent(st, copied[0], 0));
@@ -539,6 +550,27 @@ struct Engine : EngineBase {
     if (!a) return MPCMD_ERR_CONFIG;
     CK(cudaMemcpyAsync(a, d.anchor, sizeof(double) * 3 * (size_t)kp.nd, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    return MPCMD_OK;
+  }
+
+  int set_owner_tags(const int32_t* t) override {
+    if (!d.owner || !t) return MPCMD_ERR_CONFIG;
+    std::vector<uint16_t> h((size_t)kp.n);
+    for (int64_t i = 0; i < kp.n; ++i) {
+      if (t[i] < 0 || t[i] > kp.nd) return MPCMD_ERR_CONFIG;
+      h[(size_t)i] = (uint16_t)t[i];
+    }
+    CK(cudaMemcpyAsync(d.owner, h.data(), h.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return MPCMD_OK;
+  }
+
+  int get_owner_tags(int32_t* t) override {
+    if (!d.owner || !t) return MPCMD_ERR_CONFIG;
+    std::vector<uint16_t> h((size_t)kp.n);
+    CK(cudaMemcpyAsync(h.data(), d.owner, h.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int64_t i = 0; i < kp.n; ++i) t[i] = h[(size_t)i];
     return MPCMD_OK;
   }
 
@@ -975,6 +1007,7 @@ struct Engine : EngineBase {
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
     Launch<T>::build_bins(d, kp, 0, st);
     Launch<T>::init_solvent(d, kp, bounds, cfg.kT, cfg.mass, st);
+    if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)kp.n, st));
     CK(cudaStreamSynchronize(st));
     prepared = false; home_shell = false; advanced = false; n_inside = 0;
     cstep = 0; time_count = 0;
@@ -1288,6 +1321,8 @@ int Engine<T>::checkpoint(const char* path) {
   std::vector<double> anc(3 * (size_t)kp.nd);
   r = get_anchors(anc.data());
   if (r) return r;
+  std::vector<int32_t> tags(d.owner ? (size_t)n : 0);
+  if (d.owner && (r = get_owner_tags(tags.data()))) return r;
   CkptHeader h{};
   std::memcpy(h.magic, "MPCMDCK1", 8);
   h.version = 2; h.precision = (int32_t)(sizeof(T) * 8);
@@ -1295,13 +1330,15 @@ int Engine<T>::checkpoint(const char* path) {
   h.lx = kp.lx; h.ly = kp.ly; h.lz = kp.lz; h.seed = cfg.seed;
   uint64_t cs = fnv1a(buf.data(), buf.size() * 8, 1469598103934665603ull);
   cs = fnv1a(fl.data(), fl.size() * 4, cs);
-  h.checksum = fnv1a(anc.data(), anc.size() * 8, cs);
+  cs = fnv1a(anc.data(), anc.size() * 8, cs);
+  h.checksum = fnv1a(tags.data(), tags.size() * 4, cs);
   std::string tmp = std::string(path) + ".tmp";
   FILE* f = std::fopen(tmp.c_str(), "wb");
   if (!f) return MPCMD_ERR_IO;
   bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(buf.data(), 8, buf.size(), f) == buf.size() &&
             std::fwrite(fl.data(), 4, fl.size(), f) == fl.size() &&
-            std::fwrite(anc.data(), 8, anc.size(), f) == anc.size();
+            std::fwrite(anc.data(), 8, anc.size(), f) == anc.size() &&
+            std::fwrite(tags.data(), 4, tags.size(), f) == tags.size();
   ok = (std::fclose(f) == 0) && ok;
   if (!ok || std::rename(tmp.c_str(), path) != 0) { std::remove(tmp.c_str()); return MPCMD_ERR_IO; }
   return MPCMD_OK;
@@ -1322,19 +1359,26 @@ int Engine<T>::restore(const char* path) {
   std::vector<int32_t> fl((size_t)n);
   // version 1 files end with the flags; version 2 adds the rotor anchors
   std::vector<double> anc(h.version >= 2 ? 3 * (size_t)kp.nd : 0);
+  std::vector<int32_t> tags(h.version >= 2 && d.owner ? (size_t)n : 0);
   bool ok = std::fread(buf.data(), 8, buf.size(), f) == buf.size() && std::fread(fl.data(), 4, fl.size(), f) == fl.size() &&
-            std::fread(anc.data(), 8, anc.size(), f) == anc.size();
+            std::fread(anc.data(), 8, anc.size(), f) == anc.size() &&
+            std::fread(tags.data(), 4, tags.size(), f) == tags.size();
+  ok = ok && std::fgetc(f) == EOF;   // nothing left: the file matches this configuration
   std::fclose(f);
   if (!ok) return MPCMD_ERR_CHECKPOINT;
   uint64_t cs = fnv1a(buf.data(), buf.size() * 8, 1469598103934665603ull);
   cs = fnv1a(fl.data(), fl.size() * 4, cs);
-  if (h.version >= 2) cs = fnv1a(anc.data(), anc.size() * 8, cs);
+  if (h.version >= 2) {
+    cs = fnv1a(anc.data(), anc.size() * 8, cs);
+    cs = fnv1a(tags.data(), tags.size() * 4, cs);
+  }
   if (cs != h.checksum) return MPCMD_ERR_CHECKPOINT;
   int r = upload(buf.data(), buf.data() + n, buf.data() + 2 * n, buf.data() + 3 * n, buf.data() + 4 * n,
                  buf.data() + 5 * n, fl.data(), buf.data() + 6 * n, buf.data() + 6 * n + 3 * ns,
                  buf.data() + 6 * n + 6 * ns);
   if (r) return r;
   if (h.version >= 2 && (r = set_anchors(anc.data()))) return r;
+  if (!tags.empty() && (r = set_owner_tags(tags.data()))) return r;
   cstep = h.cstep;
   time_count = h.time_count;
   last_rebuild = cstep - time_count;
@@ -1429,6 +1473,16 @@ int mpcmd_set_anchors(mpcmd_ctx* ctx, const double* anchors) {
 int mpcmd_get_anchors(mpcmd_ctx* ctx, double* anchors) {
   CTX_OK(ctx);
   return ctx->e->get_anchors(anchors);
+}
+
+int mpcmd_set_owner_tags(mpcmd_ctx* ctx, const int32_t* type_b) {
+  CTX_OK(ctx);
+  return ctx->e->set_owner_tags(type_b);
+}
+
+int mpcmd_get_owner_tags(mpcmd_ctx* ctx, int32_t* type_b) {
+  CTX_OK(ctx);
+  return ctx->e->get_owner_tags(type_b);
 }
 
 int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count) {

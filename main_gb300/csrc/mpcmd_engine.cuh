@@ -102,6 +102,7 @@ struct Dev {
   double* facc;            // [ns*4] -sum F_pair (xyz) and sum of pair potentials
   double* fmot;            // [ns*4] motor-motor force and potential (j < k part)
   double* anchor;          // [nd*3] rotor anchors (motorCM)
+  uint16_t *owner, *owner2;  // [n] owner tags type_B by main index (null without owner_tags); sort buffer
   double* dpot;            // [nd] potential of each dimer at the last force evaluation
   uint32_t* bin_cnt;       // [nbins]
   uint32_t* bin_mask;      // [ceil(nbins / 32)] bit b set: bin b lists a sphere

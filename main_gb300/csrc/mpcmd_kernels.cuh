@@ -956,7 +956,8 @@ void Launch<T>::finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const St
 // flight of the next step (evolve_mod.f95:225-316) with its max_solvent_dist.
 // Extra blocks after the shell grid compute the sphere-sphere LJ forces
 // (forces_mod.f95:144-210) of the current sphere positions.
-template <typename T>
+// OWN: the owner-tag form (a template flag: the common form keeps no tag state)
+template <typename T, bool OWN>
 __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
   if (!a.rebuilt) {
@@ -1047,6 +1048,9 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
       sphl[4] = (uint16_t)(packed.z & 0xFFFFu); sphl[5] = (uint16_t)(packed.z >> 16);
       sphl[6] = (uint16_t)(packed.w & 0xFFFFu); sphl[7] = (uint16_t)(packed.w >> 16);
     }
+    // owner tag (type_B) of the particle, with owner_tags
+    uint32_t own = 0, own0 = 0;
+    if (OWN && act) own = own0 = d.owner[idx];
     T fpx[PAIRMAX], fpy[PAIRMAX], fpz[PAIRMAX];
 #pragma unroll
     for (int q = 0; q < PAIRMAX; ++q) {
@@ -1062,7 +1066,15 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
         if (d2 <= kp.cut2[t]) {
           int spc = fl & FLAG_SPECIES;
           T E = (t == 0) ? kp.eps_c[spc] : kp.eps_n[spc];
-          if (t == 0) {
+          if (OWN) {
+            // linear_periodic_no_ci/forces_mod.f95:79-121: the C sphere of
+            // motor k makes the particle a B of motor k; a B of another motor
+            // acts as an A (the slots run in ascending sphere order, the
+            // reference's motor loop)
+            const uint32_t motor = (uint32_t)(s >> 1) + 1u;
+            if (t == 0) { fl = (fl & ~FLAG_SPECIES) | 1; own = motor; E = kp.eps_c[1]; }
+            else if (spc == 1 && own != motor) E = kp.eps_n[0];
+          } else if (t == 0) {
             if (kp.catalysis == 0) {
               if (spc == 0) { fl = (fl & ~FLAG_SPECIES) | 1; E = kp.eps_c[1]; }
             } else if (spc == 0 || spc == 1) {
@@ -1120,6 +1132,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
       }
       d.sh.vx[j] = vx; d.sh.vy[j] = vy; d.sh.vz[j] = vz;
       d.sh.flag[j] = fl;
+      if (OWN && own != own0) d.owner[idx] = (uint16_t)own;
     }
   }
   if (a.advance && !a.mpc) block_max_to<T>(&d.ctr->maxmsd[(a.step + 1) & 1], msdmax);
@@ -1128,7 +1141,8 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
 template <typename T>
 void Launch<T>::force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
   int extra = (kp.ns + (TPB / 32) - 1) / (TPB / 32);
-  k_force<T><<<a.g_force + extra, TPB, 0, st>>>(d, kp, a);
+  if (kp.owner_tags) k_force<T, true><<<a.g_force + extra, TPB, 0, st>>>(d, kp, a);
+  else k_force<T, false><<<a.g_force + extra, TPB, 0, st>>>(d, kp, a);
   LAUNCH_COUNT();
 }
 
@@ -1934,6 +1948,8 @@ template <typename T>
 __device__ __forceinline__ void relabel_key(const Dev<T>& d, uint32_t key, int code) {
   const uint32_t idx = key & 0x7FFFFFFFu;
   const uint8_t f = d.p.flag[idx];
+  // B -> A clears the owner tag (linear_periodic_no_ci/reaction_simple_mod.f95:55)
+  if (d.owner && code == 0) d.owner[idx] = 0;
   if (f & FLAG_HOME_SHELL) {
     const uint32_t j = d.p.cell[idx];
     if (!chk((int64_t)j < d.sh.cap, d.ctr, 120, j)) return;
@@ -2290,7 +2306,7 @@ template <typename T>
 void Launch<T>::occupancy(int* blocks) {
   blocks[0] = blocks[1] = blocks[2] = blocks[3] = blocks[4] = blocks[5] = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], k_rebuild<T>, TPB, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], k_force<T>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], k_force<T, false>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], k_rotate_main<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], k_rebuild_far<T>, TPB, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[4], k_cells<T>, TPB, 0);
@@ -2393,6 +2409,7 @@ __global__ void k_sort_gather(Dev<T> d, KParams<T> kp) {
     d.p2.ox[q] = d.p.ox[i]; d.p2.oy[q] = d.p.oy[i]; d.p2.oz[q] = d.p.oz[i];
     d.p2.vx[q] = d.p.vx[i]; d.p2.vy[q] = d.p.vy[i]; d.p2.vz[q] = d.p.vz[i];
     d.p2.flag[q] = d.p.flag[i] & FLAG_SPECIES;
+    if (d.owner) d.owner2[q] = d.owner[i];
   }
 }
 
@@ -2407,6 +2424,7 @@ void Launch<T>::sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
   k_sort_gather<T><<<1024, TPB, 0, st>>>(d, kp);
   LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT();
   Particles<T> t = d.p; d.p = d.p2; d.p2 = t;
+  uint16_t* o = d.owner; d.owner = d.owner2; d.owner2 = o;
 }
 
 // --------------------------------------------------------------- reductions --

@@ -118,6 +118,7 @@ orc_t* orc_create(const orc_params* p) {
   o->dpos = calloc(3 * ns, 8); o->dvel = calloc(3 * ns, 8); o->dfrc = calloc(3 * ns, 8);
   o->q = calloc(3 * ns, 8);
   o->anchor = calloc(3 * ns, 8);
+  o->owner = calloc(n, 4);
   o->nbnum = calloc(ns, 8);
   o->nb = calloc(ns * o->maxnb, 8);
   o->fpair = calloc(ns * o->maxnb * 3, 8);
@@ -136,7 +137,7 @@ orc_t* orc_create(const orc_params* p) {
   o->spair = calloc(n * 2 * 3, 8);
   o->spot = calloc(n, 8);
   if (!o->x || !o->y || !o->z || !o->vx || !o->vy || !o->vz || !o->flag || !o->msd ||
-      !o->dpos || !o->dvel || !o->dfrc || !o->q || !o->anchor || !o->nbnum || !o->nb || !o->fpair ||
+      !o->dpos || !o->dvel || !o->dfrc || !o->q || !o->anchor || !o->owner || !o->nbnum || !o->nb || !o->fpair ||
       !o->pot || !o->in_list || !o->out_list || !o->newcell || !o->cm || !o->axis ||
       !o->ccount || !o->dcount || !o->dfirst || !o->affected || !o->react_box ||
       !o->fsx || !o->fsy || !o->fsz || !o->pfx || !o->pfy || !o->pfz || !o->spair || !o->spot) {
@@ -151,7 +152,7 @@ orc_t* orc_create(const orc_params* p) {
 void orc_destroy(orc_t* o) {
   if (!o) return;
   free(o->x); free(o->y); free(o->z); free(o->vx); free(o->vy); free(o->vz);
-  free(o->flag); free(o->msd); free(o->dpos); free(o->dvel); free(o->dfrc); free(o->q); free(o->anchor);
+  free(o->flag); free(o->msd); free(o->dpos); free(o->dvel); free(o->dfrc); free(o->q); free(o->anchor); free(o->owner);
   free(o->nbnum); free(o->nb); free(o->fpair); free(o->pot); free(o->in_list);
   free(o->out_list); free(o->newcell); free(o->cm); free(o->axis); free(o->ccount);
   free(o->dcount); free(o->dfirst); free(o->affected); free(o->react_box); free(o->order);
@@ -178,6 +179,7 @@ int orc_set_state(orc_t* o, const double* x, const double* y, const double* z,
   memcpy(o->x, x, n * 8); memcpy(o->y, y, n * 8); memcpy(o->z, z, n * 8);
   memcpy(o->vx, vx, n * 8); memcpy(o->vy, vy, n * 8); memcpy(o->vz, vz, n * 8);
   memcpy(o->flag, flag, n * 4);
+  memset(o->owner, 0, n * 4);
   if (o->ns > 0) {
     if (dpos) memcpy(o->dpos, dpos, 3 * o->ns * 8);
     if (dvel) memcpy(o->dvel, dvel, 3 * o->ns * 8);
@@ -195,6 +197,16 @@ int orc_set_anchors(orc_t* o, const double* anchors) {
 
 int orc_get_anchors(const orc_t* o, double* anchors) {
   if (o->nd > 0) memcpy(anchors, o->anchor, 3 * (size_t)o->nd * 8);
+  return ORC_OK;
+}
+
+int orc_set_owner(orc_t* o, const int32_t* owner) {
+  memcpy(o->owner, owner, (size_t)o->nt * 4);
+  return ORC_OK;
+}
+
+int orc_get_owner(const orc_t* o, int32_t* owner) {
+  memcpy(owner, o->owner, (size_t)o->nt * 4);
   return ORC_OK;
 }
 
@@ -376,6 +388,9 @@ int orc_sort(orc_t* o) {
 #undef PERMUTE_D
   for (int64_t j = 0; j < n; ++j) tmpi[j] = o->flag[perm[j]];
   memcpy(o->flag, tmpi, n * 4);
+  /* linear_periodic_no_ci/sort_hilbert_mod.f95:75,92 carries type_B along */
+  for (int64_t j = 0; j < n; ++j) tmpi[j] = o->owner[perm[j]];
+  memcpy(o->owner, tmpi, n * 4);
   free(cnt); free(start); free(cellid); free(perm); free(tmp); free(tmpi);
   return ORC_OK;
 }
@@ -582,6 +597,7 @@ int orc_initial(orc_t* o) {
 
   for (int s = 0; s < 3 * o->ns; ++s) { o->dvel[s] = 0.; o->dfrc[s] = 0.; }
   set_midpoint_anchors(o);
+  memset(o->owner, 0, (size_t)o->nt * 4);   /* linear_periodic_no_ci/initial_mod.f95:95,146 */
   double* vel[3] = {o->vx, o->vy, o->vz};
   double sum[3] = {0., 0., 0.};
   if (mt) {
@@ -657,6 +673,11 @@ static void lj_mot_sol(orc_t* o, int s) {
   int64_t base = (int64_t)s * o->maxnb;
   int64_t nn = o->nbnum[s];
   const int prob = o->p.catalysis == ORC_CAT_PROBABILISTIC;
+  /* owner tags (linear_periodic_no_ci/forces_mod.f95:79-121): the C sphere
+   * of motor k makes every particle in its cutoff a B of motor k; a B acts
+   * as B only on the spheres of its own motor and as A on all others */
+  const int tags = o->p.owner_tags;
+  const int32_t motor = s / 2 + 1;
   for (int64_t j = 0; j < nn; ++j) {
     int64_t i = o->nb[base + j];
     double dR[3];
@@ -664,8 +685,11 @@ static void lj_mot_sol(orc_t* o, int s) {
     if (dRsq <= cutoff2) {
       int f = o->flag[i];
       double E = eps[f & 3];
+      if (tags && !isC && f == 1 && o->owner[i] != motor) E = eps[0];
       if (isC) {
-        if (!prob) {
+        if (!prob && tags) {
+          o->flag[i] = 1; o->owner[i] = motor; E = eps[1];
+        } else if (!prob) {
           if (f == 0) { o->flag[i] = 1; E = eps[1]; }
         } else {
           if (f == 0) {
@@ -1328,7 +1352,10 @@ int orc_reaction(orc_t* o) {
       double a00 = a1;
       double prob1 = 1.0 - exp(-a00 * tau);
       double u = orc_draw(o, ORC_TAG_RXN, (uint32_t)c, 0, step, 0);
-      if (0. < u && u <= prob1) o->flag[o->dfirst[4 * c + 1]] = 0;
+      if (0. < u && u <= prob1) {
+        o->flag[o->dfirst[4 * c + 1]] = 0;
+        o->owner[o->dfirst[4 * c + 1]] = 0;   /* linear_periodic_no_ci/reaction_simple_mod.f95:55 */
+      }
     }
   } else if (o->p.kinetics == ORC_KIN_SELKOV) {
     static const int target_species[7] = {-1, 3, 0, 0, 1, 1, 3};

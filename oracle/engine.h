@@ -15,6 +15,7 @@ struct orc {
   double *dpos, *dvel, *dfrc; /* [ns*3]                                            */
   double* q;                  /* RATTLE q vectors [ns*3]                           */
   double* anchor;             /* rotor anchors motorCM [nd*3]                      */
+  int32_t* owner;             /* owner tags type_B [nt]                            */
   int64_t maxnb;
   int64_t* nbnum;             /* [ns]                                              */
   int64_t* nb;                /* [ns*maxnb]                                        */

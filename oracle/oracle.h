@@ -85,7 +85,10 @@ typedef struct orc_params {
   int32_t variant;           /* ORC_VARIANT_*                                       */
   int32_t layout;            /* ORC_LAYOUT_*: dimer placement of orc_initial        */
   int32_t layout_rows, layout_cols;  /* numrows, numcols of the grid layout         */
-  int32_t reserved[2];
+  int32_t owner_tags;        /* 1: B particles carry the motor that made them and
+                                act as A on every other motor (type_B of
+                                linear_periodic_no_ci/forces_mod.f95:79-121)     */
+  int32_t reserved;
   double tether_k, tether_z; /* k_harm and zdimeq of the harmonic z tether          */
   double layout_sep;         /* sep: gap between neighbouring motors of a layout    */
 } orc_params;
@@ -122,6 +125,10 @@ int orc_get_state(const orc_t* o, double* x, double* y, double* z,
  * them to the midpoints of the dimers they receive or place. */
 int orc_set_anchors(orc_t* o, const double* anchors);
 int orc_get_anchors(const orc_t* o, double* anchors);
+/* Owner tags (type_B): 1-based motor number of the C sphere that made a B
+ * particle, 0 for none; [n_solvent].  orc_set_state and orc_initial clear them. */
+int orc_set_owner(orc_t* o, const int32_t* owner);
+int orc_get_owner(const orc_t* o, int32_t* owner);
 int orc_set_cell_order(orc_t* o, const int32_t* order, int64_t n);
 int orc_set_cstep(orc_t* o, int64_t cstep, int32_t time_count);
 

@@ -26,7 +26,7 @@ PARAM_FIELDS = [
     ("rot_angle", _D), ("md_dt", _D), ("mpc_dt", _D), ("k", _D * 6),
     ("engine_only", _I32 * 2),
     ("variant", _I32), ("layout", _I32), ("layout_rows", _I32), ("layout_cols", _I32),
-    ("reserved", _I32 * 2), ("tether_k", _D), ("tether_z", _D), ("layout_sep", _D),
+    ("owner_tags", _I32), ("reserved", _I32), ("tether_k", _D), ("tether_z", _D), ("layout_sep", _D),
 ]
 
 
@@ -65,6 +65,8 @@ def lib():
             "orc_set_rng": (C.c_int, [P, C.c_int, C.c_uint32]),
             "orc_set_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
             "orc_get_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
+            "orc_set_owner": (C.c_int, [P, ip]),
+            "orc_get_owner": (C.c_int, [P, ip]),
             "orc_set_anchors": (C.c_int, [P, dp]),
             "orc_get_anchors": (C.c_int, [P, dp]),
             "orc_set_cell_order": (C.c_int, [P, ip, C.c_int64]),
@@ -232,6 +234,17 @@ class Oracle:
         a = np.zeros((max(self.ns // 2, 1), 3))
         lib().orc_get_anchors(self.h, _ptr(a, C.c_double))
         return a[: self.ns // 2]
+
+    def set_owner(self, owner):
+        a = np.ascontiguousarray(owner, dtype=np.int32)
+        if a.size != self.n:
+            raise ValueError("owner tags: one per solvent particle")
+        self._check(lib().orc_set_owner(self.h, _ptr(a, C.c_int32)), "set_owner")
+
+    def get_owner(self):
+        a = np.zeros(self.n, dtype=np.int32)
+        lib().orc_get_owner(self.h, _ptr(a, C.c_int32))
+        return a
 
     def set_cell_order(self, order):
         a = np.ascontiguousarray(order, dtype=np.int32)

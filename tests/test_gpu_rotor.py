@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from gpu_helpers import assert_close, pair
-from main_gb300 import Engine, config
+from main_gb300 import Engine, MpcmdError, config
 from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -17,6 +17,9 @@ pytestmark = pytest.mark.gpu
 CASES = {
     "rot": lambda prec, **kw: config.workload("rot", scale=0.5, precision=prec, **kw),
     "rot_line": lambda prec, **kw: config.workload("rot_line", scale=0.25, precision=prec, **kw),
+    # linear_periodic_no_ci: owner tags, a sort inside the run, a fast B -> A reaction
+    "rot_owner": lambda prec, **kw: config.workload("rot_owner", scale=0.25, precision=prec, sort_every=40,
+                                                    k=[0.5, 0, 0, 0, 0, 0], **kw),
 }
 
 
@@ -45,6 +48,10 @@ def test_rotor_trajectory_fp64(case):
         o.run(chunk)
         e.run(chunk)
         assert_close(e.download_state(), o.get_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)
+        if cfg["owner_tags"]:
+            assert np.array_equal(e.get_owner_tags(), o.get_owner())
+    if cfg["owner_tags"]:
+        assert e.get_owner_tags().any()
     oo, oe = o.observables(), e.observables()
     assert np.array_equal(oo["species_count"], oe["species_count"])
     assert abs(oo["potential"] - oe["potential"]) <= 1e-9 * max(1.0, abs(oo["potential"]))
@@ -64,6 +71,8 @@ def test_rotor_trajectory_fp32(case):
     o.run(100)
     e.run(100)
     assert_close(e.download_state(), o.get_state(), cfg, pos=2e-4, vel=2e-3, flags=0.999, dimer=1e-4)
+    if cfg["owner_tags"]:
+        assert (e.get_owner_tags() == o.get_owner()).mean() >= 0.999
 
 
 def test_set_anchors_and_checkpoint(tmp_path):
@@ -93,3 +102,28 @@ def test_set_anchors_and_checkpoint(tmp_path):
     e.run(20)
     f.run(20)
     assert_close(f.download_state(), e.download_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)
+
+
+def test_owner_tags_exchange_checkpoint_and_config(tmp_path):
+    cfg = CASES["rot_owner"](64)
+    o, e = pair(cfg)
+    assert not e.get_owner_tags().any()
+    tags = (np.arange(cfg["n_solvent"]) % (cfg["n_dimers"] + 1)).astype(np.int32)
+    e.set_owner_tags(tags)
+    assert np.array_equal(e.get_owner_tags(), tags)
+    with pytest.raises(MpcmdError):
+        e.set_owner_tags(np.full(cfg["n_solvent"], cfg["n_dimers"] + 1, dtype=np.int32))
+    e.prepare()
+    e.run(30)
+    path = str(tmp_path / "owner.ck")
+    e.checkpoint(path)
+    f = Engine(cfg)
+    f.restore(path)
+    assert np.array_equal(f.get_owner_tags(), e.get_owner_tags())
+    # a context without owner tags refuses the calls; owner tags need the
+    # deterministic catalysis of the rotor codes
+    plain = Engine(CASES["rot_line"](64))
+    with pytest.raises(MpcmdError):
+        plain.get_owner_tags()
+    with pytest.raises(MpcmdError):
+        Engine(dict(cfg, catalysis=config.CAT_PROBABILISTIC))

@@ -155,3 +155,71 @@ def test_rotational_decks_parse():
     assert (c["lx"], c["n_dimers"], c["layout"]) == (256, 26, config.LAYOUT_LINE)
     pitch = c["dcn"] + 2.0 * c["rc"] * 2.0 ** (1.0 / 6.0)
     assert abs(c["layout_sep"] - (256 - 26 * pitch) / 26) < 1e-12
+
+
+def _two_rotor_state(cfg, placed):
+    """Two rotors along x at the tether plane and solvent particles `placed`
+    [(x, y, z, species, owner)], the rest far above the rotors."""
+    n = cfg["n_solvent"]
+    st = {k: np.zeros(n) for k in ("vx", "vy", "vz")}
+    st["x"] = 1.0 + (np.arange(n) % 60).astype(float)
+    st["y"] = 0.5 + (np.arange(n) // 60 % 15).astype(float)
+    st["z"] = np.full(n, cfg["lz"] - 0.5)
+    st["flag"] = np.zeros(n, dtype=np.int32)
+    owner = np.zeros(n, dtype=np.int32)
+    for i, (x, y, z, sp, ow) in enumerate(placed):
+        st["x"][i], st["y"][i], st["z"][i], st["flag"][i], owner[i] = x, y, z, sp, ow
+    zc = cfg["tether_z"]
+    st["dpos"] = np.array([[10.0, 8.0, zc], [15.0, 8.0, zc], [40.0, 8.0, zc], [45.0, 8.0, zc]])
+    st["dvel"] = np.zeros((4, 3))
+    return st, owner
+
+
+@pytest.mark.parametrize("tags", [0, 1])
+def test_owner_tags_select_the_interaction(tags):
+    # linear_periodic_no_ci/forces_mod.f95:79-121: a B of motor 1 near the N
+    # sphere of motor 2 acts as an A there; a particle in the C cutoff of
+    # motor 2 becomes a B of motor 2
+    cfg = rotor_cfg("rot_owner", n_dimers=2, owner_tags=tags, n_solvent=64, init_count=[64, 0, 0, 0],
+                    sort_every=0)
+    o = O.Oracle(cfg, threads=1)
+    st, owner = _two_rotor_state(cfg, [(45.0, 10.1, cfg["tether_z"], 1, 1),
+                                       (40.0, 10.0, cfg["tether_z"], 1, 1)])
+    o.set_state(st)
+    o.set_owner(owner)
+    o.prepare()
+    o.run(1)
+    got = o.get_state()
+    f = got["dforce"]
+    # the N sphere of motor 2 (sphere 3) feels only particle 0, along y
+    if tags:
+        assert np.array_equal(o.get_owner()[:2], [1, 2])
+        f_tag = f[3, 1]
+        ref = O.Oracle(dict(cfg, owner_tags=0), threads=1)
+        ref.set_state(st)
+        ref.prepare()
+        ref.run(1)
+        fb = ref.get_state()["dforce"][3, 1]
+        assert f_tag != 0.0
+        assert abs(f_tag / fb - cfg["eps_n"][0] / cfg["eps_n"][1]) < 1e-12
+    else:
+        assert np.array_equal(o.get_owner()[:2], [1, 1])   # untouched without tags
+    assert np.array_equal(got["flag"][:2], [1, 1])
+
+
+def test_owner_tags_follow_the_particles():
+    # A particles carry no tag and every B one of a motor, through catalysis,
+    # the B -> A reaction and the sort (sort_hilbert_mod.f95:75)
+    cfg = rotor_cfg("rot_owner", sort_every=40, k=[0.5, 0, 0, 0, 0, 0])
+    o = O.Oracle(cfg, threads=4)
+    o.initial()
+    assert not o.get_owner().any()
+    o.prepare()
+    o.run(6 * cfg["mpc_every"])
+    st, own = o.get_state(), o.get_owner()
+    assert np.all(own[st["flag"] == 0] == 0)
+    b = st["flag"] == 1
+    assert b.sum() > 0
+    assert np.all((own[b] >= 1) & (own[b] <= cfg["n_dimers"]))
+    # every motor has made some of them
+    assert set(np.unique(own[b])) == set(range(1, cfg["n_dimers"] + 1))
