@@ -25,6 +25,8 @@ module mpcmd_shim
   integer(c_int32_t), parameter, public :: MPCMD_EXCL_PARTICLE = 0, MPCMD_EXCL_CELLS = 1
   integer(c_int32_t), parameter, public :: MPCMD_CAT_DETERMINISTIC = 0, MPCMD_CAT_PROBABILISTIC = 1
   integer(c_int32_t), parameter, public :: MPCMD_PREC_FP32 = 32, MPCMD_PREC_FP64 = 64
+  integer(c_int32_t), parameter, public :: MPCMD_VARIANT_MOTOR = 0, MPCMD_VARIANT_ROTOR = 1
+  integer(c_int32_t), parameter, public :: MPCMD_LAYOUT_RANDOM = 0, MPCMD_LAYOUT_GRID = 1, MPCMD_LAYOUT_LINE = 2
 
   ! struct mpcmd_config
   type, bind(C), public :: mpcmd_config
