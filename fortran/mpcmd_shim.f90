@@ -89,7 +89,7 @@ module mpcmd_shim
   end type mpcmd_obs
 
   public :: mpcmd_create, mpcmd_destroy, mpcmd_error_string, mpcmd_upload_state, mpcmd_download_state
-  public :: mpcmd_set_step, mpcmd_initial, mpcmd_prepare, mpcmd_step, mpcmd_evolve, mpcmd_run
+  public :: mpcmd_set_step, mpcmd_initial, mpcmd_prepare, mpcmd_prepare_restart, mpcmd_step, mpcmd_evolve, mpcmd_run
   public :: mpcmd_sort, mpcmd_rebuild_lists, mpcmd_distribute, mpcmd_mpc_rotation, mpcmd_reaction
   public :: mpcmd_observables, mpcmd_checkpoint, mpcmd_restore, mpcmd_set_cell_order
   public :: mpcmd_concentration, mpcmd_dimer_axes, mpcmd_set_anchors, mpcmd_get_anchors
@@ -169,6 +169,10 @@ module mpcmd_shim
       type(c_ptr), value :: ctx
     end function
     integer(c_int) function mpcmd_prepare(ctx) bind(C, name="mpcmd_prepare")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function mpcmd_prepare_restart(ctx) bind(C, name="mpcmd_prepare_restart")
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
     end function

@@ -156,6 +156,10 @@ int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count);
 /* Reference call surface ----------------------------------------------- */
 int mpcmd_initial(mpcmd_ctx* ctx);        /* initial_mod.f95:6-355                 */
 int mpcmd_prepare(mpcmd_ctx* ctx);        /* main_pattern.f95:168-187              */
+/* restart_mod.f95:415-528: mpcmd_prepare, then the forces of the state (pair
+ * forces for the first half kick, catalysis, sphere totals) without a kick.
+ * mpcmd_prepare after mpcmd_restore does the same. */
+int mpcmd_prepare_restart(mpcmd_ctx* ctx);
 int mpcmd_step(mpcmd_ctx* ctx);           /* main_pattern.f95:203-225, one step    */
 int mpcmd_evolve(mpcmd_ctx* ctx);         /* evolve_mod.f95:6-732, one MD step only */
 int mpcmd_run(mpcmd_ctx* ctx, int64_t nsteps);  /* nsteps main-loop iterations     */

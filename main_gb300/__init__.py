@@ -69,6 +69,7 @@ SIGNATURES = {
     "mpcmd_set_step": (C.c_int, [_P, C.c_int64, C.c_int32]),
     "mpcmd_initial": (C.c_int, [_P]),
     "mpcmd_prepare": (C.c_int, [_P]),
+    "mpcmd_prepare_restart": (C.c_int, [_P]),
     "mpcmd_step": (C.c_int, [_P]),
     "mpcmd_evolve": (C.c_int, [_P]),
     "mpcmd_run": (C.c_int, [_P, C.c_int64]),
@@ -248,6 +249,9 @@ class Engine:
 
     def prepare(self):
         self._c(lib().mpcmd_prepare(self.h), "prepare")
+
+    def prepare_restart(self):
+        self._c(lib().mpcmd_prepare_restart(self.h), "prepare_restart")
 
     def step(self):
         self._c(lib().mpcmd_step(self.h), "step")

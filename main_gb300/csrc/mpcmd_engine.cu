@@ -130,6 +130,7 @@ struct EngineBase {
   virtual int set_step(int64_t cstep, int32_t tc) = 0;
   virtual int initial() = 0;
   virtual int prepare() = 0;
+  virtual int prepare_restart() = 0;
   virtual int run(int64_t nsteps, bool with_mpc) = 0;
   virtual int sort_stage() = 0;
   virtual int rebuild_stage() = 0;
@@ -188,6 +189,8 @@ struct Engine : EngineBase {
   int64_t last_full = 0;   // step of the last rebuild that wrote every particle
   int64_t force_rebuild_step = -1;
   bool prepared = false, home_shell = false, advanced = false;
+  // the next prepare evaluates the forces of the state, as restart_mod.f95 does
+  bool restart_pending = false;
   // the watch list of the last collision is valid (no full pass or stage call since)
   bool watch_valid = false;
   double w3 = 1.0;
@@ -526,6 +529,7 @@ struct Engine : EngineBase {
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
     CK(cudaStreamSynchronize(st));
     prepared = false; home_shell = false; advanced = false; n_inside = 0;
+    restart_pending = false;
     return MPCMD_OK;
   }
 
@@ -605,7 +609,8 @@ struct Engine : EngineBase {
       CK(cudaEventRecord(copied[b], cst));
     }
     if (flag) {
-      Launch<T>::download_flag(d, kp, d.staging_i, st);
+      Launch<T>::download_flag(d, kp, d.staging_i, time_count, (int)(last_rebuild - last_full), current ? 1 : 0,
+                               st);
       CK(cudaEventRecord(done[0], st));
       CK(cudaStreamWaitEvent(cst, done[0], 0));
       CK(cudaMemcpyAsync(flag, d.staging_i, sizeof(int32_t) * kp.n, cudaMemcpyDeviceToHost, cst));
@@ -733,8 +738,21 @@ struct Engine : EngineBase {
     if (h.status) return dev_status_to_api(h.status);
     if (kp.ns == 0) std::swap(d.sh, d.sh2);   // (with spheres sort_shell filled d.sh)
     // the first half kick of the run uses zero pair forces, as after
-    // initial_mod.f95 (FpairX = 0)
+    // initial_mod.f95 (FpairX = 0), or after a restart the forces of the
+    // state (restart_mod.f95:415-528: pair forces, catalysis, sphere totals;
+    // no kick)
     CK(cudaMemsetAsync(d.sh.pf, 0, sizeof(T) * 3 * PAIRMAX * (size_t)d.sh.cap, st));
+    if (restart_pending) {
+      StepArgs f = args(cstep);
+      f.forces_only = 1;
+      f.rebuilt = 1;
+      Launch<T>::force(d, kp, f, st);
+      Launch<T>::sphere_totals(d, kp, w3, st);
+      Counters hf;
+      if ((r = read_counters(hf))) return r;
+      if (hf.status) return dev_status_to_api(hf.status);
+      restart_pending = false;
+    }
     CK(cudaStreamSynchronize(st));
     n_inside = h.n_inside;
     time_penetrate = h.time_penetrate;
@@ -744,6 +762,11 @@ struct Engine : EngineBase {
     home_shell = true;
     prepared = true;
     return MPCMD_OK;
+  }
+
+  int prepare_restart() override {
+    restart_pending = true;
+    return prepare();
   }
 
   int handle_abort(int step) {
@@ -1010,6 +1033,7 @@ struct Engine : EngineBase {
     if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)kp.n, st));
     CK(cudaStreamSynchronize(st));
     prepared = false; home_shell = false; advanced = false; n_inside = 0;
+    restart_pending = false;
     cstep = 0; time_count = 0;
     Counters h;
     int r = read_counters(h);
@@ -1378,6 +1402,7 @@ int Engine<T>::restore(const char* path) {
                  buf.data() + 6 * n + 6 * ns);
   if (r) return r;
   if (h.version >= 2 && (r = set_anchors(anc.data()))) return r;
+  restart_pending = true;
   if (!tags.empty() && (r = set_owner_tags(tags.data()))) return r;
   cstep = h.cstep;
   time_count = h.time_count;
@@ -1473,6 +1498,11 @@ int mpcmd_set_anchors(mpcmd_ctx* ctx, const double* anchors) {
 int mpcmd_get_anchors(mpcmd_ctx* ctx, double* anchors) {
   CTX_OK(ctx);
   return ctx->e->get_anchors(anchors);
+}
+
+int mpcmd_prepare_restart(mpcmd_ctx* ctx) {
+  CTX_OK(ctx);
+  return ctx->e->prepare_restart();
 }
 
 int mpcmd_set_owner_tags(mpcmd_ctx* ctx, const int32_t* type_b) {

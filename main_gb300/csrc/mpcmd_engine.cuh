@@ -138,6 +138,7 @@ struct StepArgs {
   int mpc;             // this step ends with a collision
   int advance;         // fuse kick1 + stream of the next step
   int rebuilt;         // a rebuild ran in this step
+  int forces_only;     // k_force: pair forces, catalysis and sphere sums without the kicks (a restart)
   int merge_only;      // rebuild pass: lazy-stream and merge only, no lists
   int grid;            // persistent grid size of the light kernels
   int g_rebuild;       // SMs x resident blocks of k_rebuild, k_force, k_rotate_main
@@ -163,7 +164,8 @@ struct Launch {
   static void upload_flag(const Dev<T>& d, const KParams<T>& kp, const int32_t* src, cudaStream_t st);
   static void download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
                                int tc_defer, int current, cudaStream_t st);
-  static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st);
+  static void download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, int tc, int tc_defer,
+                            int current, cudaStream_t st);
   static void update_srel(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   // tc_defer > 0: bins also reach every sphere that a deferred particle,
   // stored tc_defer steps ago, can be near now (for the rebuild fast path)
@@ -179,6 +181,7 @@ struct Launch {
   // free-flight members to the main home and compacts the rest into d.sh2
   // (the caller then swaps d.sh and d.sh2)
   static void advance(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);
+  static void sphere_totals(const Dev<T>& d, const KParams<T>& kp, double w3, cudaStream_t st);
   static void dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode,
                     double w3, int rattle_max, cudaStream_t st);
   static void affected(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st);

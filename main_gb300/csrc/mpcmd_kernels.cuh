@@ -343,16 +343,37 @@ void Launch<T>::concentration(const Dev<T>& d, const KParams<T>& kp, int tc, int
   LAUNCH_COUNT();
 }
 
+// Species of every particle.  In the reference's view (outside particles at
+// the last rebuild) these are the stored species: a lagging particle of that
+// view cannot reach a wall before its lag ends.  With `current` the outside
+// particles written at the last rebuild are streamed over the lag as in
+// k_download, so a reactive-floor hit in that time (reactive_grid_mod.f95:
+// 103-151) changes the species it reports.
 template <typename T>
-__global__ void k_download_flag(Particles<T> p, KParams<T> kp, int32_t* out) {
+__global__ void k_download_flag(Particles<T> p, KParams<T> kp, const uint8_t* react_box, int32_t* out, int tc,
+                                int tc_defer, int current) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride)
-    out[i] = p.flag[i] & FLAG_SPECIES;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
+    uint8_t f = p.flag[i];
+    if (current) {
+      int lag = 0;
+      if (f & FLAG_PASSIVE) lag = tc;
+      else if (!(f & (FLAG_INLIST | FLAG_FRESH | FLAG_HOME_SHELL))) lag = tc_defer + tc;
+      else if (!(f & (FLAG_INLIST | FLAG_HOME_SHELL))) lag = tc;
+      if (lag > 0) {
+        uint32_t c = p.cell[i];
+        T ox = p.ox[i], oy = p.oy[i], oz = p.oz[i], vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
+        stream_one(kp, react_box, c, ox, oy, oz, vx, vy, vz, f, true, lag);
+      }
+    }
+    out[i] = f & FLAG_SPECIES;
+  }
 }
 
 template <typename T>
-void Launch<T>::download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, cudaStream_t st) {
-  k_download_flag<T><<<1024, TPB, 0, st>>>(d.p, kp, out);
+void Launch<T>::download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, int tc, int tc_defer,
+                              int current, cudaStream_t st) {
+  k_download_flag<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, tc, tc_defer, current);
   LAUNCH_COUNT();
 }
 
@@ -1096,7 +1117,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
       const T h2 = kp.hIM[fl & FLAG_SPECIES];
 #pragma unroll
       for (int q = 0; q < PAIRMAX; ++q) {
-        if (q >= np) break;
+        if (q >= np || a.forces_only) break;
         vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
       }
       if (a.mpc) {
@@ -1841,6 +1862,37 @@ __global__ void k_dimer_split(Dev<T> d, KParams<T> kp, StepArgs a, int mode, dou
     }
   }
   if (live && c == 0 && iters) atomicAdd(&d.ctr->rattle_iters, iters);
+}
+
+// Sphere force totals and dimer potentials of a restart (restart_mod.f95:
+// 505-528), one thread per dimer: the same sums as the first stage of
+// k_dimer / k_dimer_split / k_rotor (pair sums, motor-motor forces, the wall
+// or the rotor tether), with no RATTLE.
+template <typename T>
+__global__ void k_sphere_totals(Dev<T> d, KParams<T> kp, double w3) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kp.nd) return;
+  const bool per = kp.geometry == 1;
+  double pot = 0.;
+  for (int i = 0; i < 2; ++i) {
+    const int s = 2 * k + i;
+    double fw = 0., pw = 0.;
+    if (kp.rotor) harmonic_tether(d.dpos[3 * s + 2], kp.tether_z, kp.tether_k, fw, pw);
+    else if (!per) lj_wall(kp, d.dpos[3 * s + 2], i == 0 ? kp.rwc : kp.rwn, w3, fw, pw);
+    d.dfrc[3 * s + 0] = d.facc[4 * s + 0] + d.fmot[4 * s + 0];
+    d.dfrc[3 * s + 1] = d.facc[4 * s + 1] + d.fmot[4 * s + 1];
+    d.dfrc[3 * s + 2] = d.facc[4 * s + 2] + d.fmot[4 * s + 2] + fw;
+    pot += d.facc[4 * s + 3] + d.fmot[4 * s + 3] + pw;
+    d.facc[4 * s + 0] = 0.; d.facc[4 * s + 1] = 0.; d.facc[4 * s + 2] = 0.; d.facc[4 * s + 3] = 0.;
+  }
+  d.dpot[k] = pot;
+}
+
+template <typename T>
+void Launch<T>::sphere_totals(const Dev<T>& d, const KParams<T>& kp, double w3, cudaStream_t st) {
+  if (kp.nd == 0) return;
+  k_sphere_totals<T><<<(kp.nd + 63) / 64, 64, 0, st>>>(d, kp, w3);
+  LAUNCH_COUNT();
 }
 
 template <typename T>

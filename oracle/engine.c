@@ -659,6 +659,16 @@ int orc_prepare(orc_t* o) {
   return o->status;
 }
 
+/* restart_mod.f95:415-528: after the lists of a restart, the forces of the
+ * restart state (pair forces for the first half kick, catalysis, sphere
+ * totals); no kick. */
+static void compute_forces(orc_t* o);
+int orc_restart_forces(orc_t* o) {
+  if (!o->prepared) return o->status = ORC_ERR_STATE;
+  compute_forces(o);
+  return o->status;
+}
+
 /* ---------------------------------------------------------------- forces -- */
 /* forces_mod.f95:6-140 (LJ_mot_sol) for sphere s over its list, with the
  * catalytic rule of the run (collective :79-92 or ForcesMD_SelkovDimer:302-339). */
@@ -990,40 +1000,16 @@ static void kick_lists(orc_t* o) {
   }
 }
 
-static void evolve(orc_t* o) {
-  const double dt = o->p.md_dt;
+/* evolve_mod.f95:441-452 (pair forces of the lists in use cleared), :567-602
+ * (sphere-solvent LJ with catalysis, motor-motor LJ, the wall, or the rotor
+ * tether of rotational_code/2d_array/evolve_mod.f95:515-531) and :605-636
+ * (sphere totals and the potential); restart_mod.f95:415-528 runs the same
+ * evaluation at a restart. */
+static void compute_forces(orc_t* o) {
   const double cut = pow(2.0, 1.0 / 6.0);
-  kick_lists(o);
-  /* stream inside particles :258-315 */
-#pragma omp parallel for schedule(static)
-  for (int64_t j = 0; j < o->n_in; ++j) {
-    int64_t i = o->in_list[j];
-    stream_particle(o, i, dt, 1, 0);
-    o->msd[i] = o->msd[i] + (o->vx[i] * o->vx[i] + o->vy[i] * o->vy[i] + o->vz[i] * o->vz[i]) * (dt * dt);
-  }
-  /* RATTLE positions :320-417 */
   const int rotor = o->p.variant == ORC_VARIANT_ROTOR;
-  for (int k = 0; k < o->nd; ++k) {
-    if (rotor) rattle_positions_rotor(o, k);
-    else rattle_positions(o, k);
-  }
-  /* zero sphere forces :424-455 */
   for (int j = 0; j < 3 * o->ns; ++j) o->dfrc[j] = 0.;
   o->tpot = 0.;
-  /* rebuild test :457-465 */
-  double maxv = o->msd[0];
-  for (int64_t i = 0; i < o->nt; ++i) if (o->msd[i] > maxv) maxv = o->msd[i];
-  int mpc_step = (o->cstep % o->p.mpc_every) == 0;
-  if (maxv > (0.5 * o->p.skin) * (0.5 * o->p.skin) || o->time_count == o->time_penetrate || mpc_step) {
-#pragma omp parallel for schedule(static)
-    for (int64_t j = 0; j < o->n_out; ++j) stream_particle(o, o->out_list[j], dt, o->time_count, 1);
-    if (o->p.sort_every > 0 && o->cstep % o->p.sort_every == 0) orc_sort(o);
-    orc_rebuild_lists(o);
-    for (int64_t i = 0; i < o->nt; ++i) o->msd[i] = 0.;
-    compute_time_penetrate(o);
-    o->time_count = 0;
-    o->n_rebuilds++;
-  }
   /* clear pair forces for the lists in use */
   for (int s = 0; s < o->ns; ++s) {
     int64_t base = (int64_t)s * o->maxnb;
@@ -1095,6 +1081,41 @@ static void evolve(orc_t* o) {
       o->tpot += tp;
     }
   free(fmot); free(fmotpot); free(fwall); free(wpot);
+}
+
+static void evolve(orc_t* o) {
+  const double dt = o->p.md_dt;
+  const double cut = pow(2.0, 1.0 / 6.0);
+  kick_lists(o);
+  /* stream inside particles :258-315 */
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < o->n_in; ++j) {
+    int64_t i = o->in_list[j];
+    stream_particle(o, i, dt, 1, 0);
+    o->msd[i] = o->msd[i] + (o->vx[i] * o->vx[i] + o->vy[i] * o->vy[i] + o->vz[i] * o->vz[i]) * (dt * dt);
+  }
+  /* RATTLE positions :320-417 */
+  const int rotor = o->p.variant == ORC_VARIANT_ROTOR;
+  for (int k = 0; k < o->nd; ++k) {
+    if (rotor) rattle_positions_rotor(o, k);
+    else rattle_positions(o, k);
+  }
+  /* (sphere forces :424-455 are zeroed by compute_forces) */
+  /* rebuild test :457-465 */
+  double maxv = o->msd[0];
+  for (int64_t i = 0; i < o->nt; ++i) if (o->msd[i] > maxv) maxv = o->msd[i];
+  int mpc_step = (o->cstep % o->p.mpc_every) == 0;
+  if (maxv > (0.5 * o->p.skin) * (0.5 * o->p.skin) || o->time_count == o->time_penetrate || mpc_step) {
+#pragma omp parallel for schedule(static)
+    for (int64_t j = 0; j < o->n_out; ++j) stream_particle(o, o->out_list[j], dt, o->time_count, 1);
+    if (o->p.sort_every > 0 && o->cstep % o->p.sort_every == 0) orc_sort(o);
+    orc_rebuild_lists(o);
+    for (int64_t i = 0; i < o->nt; ++i) o->msd[i] = 0.;
+    compute_time_penetrate(o);
+    o->time_count = 0;
+    o->n_rebuilds++;
+  }
+  compute_forces(o);
   kick_lists(o);
   for (int k = 0; k < o->nd; ++k) {
     if (rotor) rattle_velocities_rotor(o, k);

@@ -127,6 +127,9 @@ int orc_set_anchors(orc_t* o, const double* anchors);
 int orc_get_anchors(const orc_t* o, double* anchors);
 /* Owner tags (type_B): 1-based motor number of the C sphere that made a B
  * particle, 0 for none; [n_solvent].  orc_set_state and orc_initial clear them. */
+/* restart_mod.f95:415-528: after orc_prepare, evaluate the forces of the
+ * state (pair forces for the first half kick, catalysis, sphere totals). */
+int orc_restart_forces(orc_t* o);
 int orc_set_owner(orc_t* o, const int32_t* owner);
 int orc_get_owner(const orc_t* o, int32_t* owner);
 int orc_set_cell_order(orc_t* o, const int32_t* order, int64_t n);

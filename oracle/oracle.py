@@ -65,6 +65,7 @@ def lib():
             "orc_set_rng": (C.c_int, [P, C.c_int, C.c_uint32]),
             "orc_set_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
             "orc_get_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
+            "orc_restart_forces": (C.c_int, [P]),
             "orc_set_owner": (C.c_int, [P, ip]),
             "orc_get_owner": (C.c_int, [P, ip]),
             "orc_set_anchors": (C.c_int, [P, dp]),
@@ -258,6 +259,9 @@ class Oracle:
 
     def prepare(self):
         return self._check(lib().orc_prepare(self.h), "prepare")
+
+    def restart_forces(self):
+        return self._check(lib().orc_restart_forces(self.h), "restart_forces")
 
     def step(self):
         return self._check(lib().orc_step(self.h), "step")

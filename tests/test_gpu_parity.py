@@ -174,12 +174,10 @@ def test_checkpoint_roundtrip(tmp_path):
     f.restore(path)
     c1, c2 = e.counters(), f.counters()
     assert c1["cstep"] == c2["cstep"]
-    # the file holds every particle at the checkpoint step: the restored
-    # context equals the original one brought to that step by mpcmd_prepare,
-    # and both go on alike
-    e.prepare()
-    ref, got = e.download_state(), f.download_state()
-    assert_close(got, ref, cfg, pos=1e-12, vel=1e-12, flags=1.0, dimer=0.0)
+    # the file holds every particle at the checkpoint step; the restored
+    # context, prepared as restart_mod.f95 does (forces of the state, no
+    # kick), goes on as the original one; at the collision step 100 every
+    # particle is at that step in both views
     f.prepare()
     e.run(40)
     f.run(40)
@@ -230,3 +228,51 @@ def test_displacement_rebuild_trigger_fp64():
     # displacement test first and both codes agree on the schedule
     assert ob["time_penetrate"] == c["time_penetrate"] and c["time_penetrate"] < 5
     assert c["last_rebuild"] == ob["cstep"] - ob["time_count"]
+
+
+@pytest.mark.parametrize("case", ["c1", "c2"])
+def test_restart_continues_the_run_fp64(case):
+    """mpcmd_checkpoint at step 60, mpcmd_restore and mpcmd_prepare (the
+    restart forces of restart_mod.f95:415-528): the restored context and the
+    uninterrupted one agree at the collision steps 100 and 150."""
+    import tempfile, os
+    cfg = CASES[case](64)
+    o, e = pair(cfg)
+    e.prepare()
+    e.run(60)
+    path = os.path.join(tempfile.mkdtemp(prefix="mpcmd_ck_"), "ck.bin")
+    e.checkpoint(path)
+    f = Engine(cfg)
+    f.restore(path)
+    f.prepare()
+    steps = 100 - 60 if cfg["mpc_every"] == 50 else (-60) % cfg["mpc_every"] + cfg["mpc_every"]
+    for chunk in (steps, cfg["mpc_every"]):
+        e.run(chunk)
+        f.run(chunk)
+        assert_close(f.download_state(), e.download_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)
+
+
+@pytest.mark.parametrize("case", ["c1", "c2"])
+def test_prepare_restart_matches_oracle(case):
+    """A mid-run state started with mpcmd_prepare_restart and with the
+    oracle's prepare + restart_forces: forces of the state, then 60 steps."""
+    cfg = CASES[case](64)
+    o, e = pair(cfg)
+    o.prepare()
+    o.run(37)
+    st = o.get_state()
+    r = Oracle(cfg)
+    r.set_state(st)
+    r.set_cstep(37, 0)
+    r.set_cell_order(e.cell_order())
+    r.prepare()
+    r.restart_forces()
+    e.upload_state(st)
+    e.set_step(37, 0)
+    e.prepare_restart()
+    se, so = e.download_state(), r.get_state()
+    assert np.abs(se["dforce"] - so["dforce"]).max() <= 1e-9 * max(1.0, np.abs(so["dforce"]).max())
+    assert np.array_equal(se["flag"], so["flag"])
+    r.run(63)
+    e.run(63)
+    assert_close(e.download_state(), r.get_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)

@@ -95,12 +95,11 @@ def test_set_anchors_and_checkpoint(tmp_path):
     f = Engine(cfg)
     f.restore(path)
     assert np.array_equal(f.get_anchors(), new)
-    # a restart (restart_mod.f95) prepares the lists again: the restored
-    # context and the original one, both prepared at the same step, go on alike
-    e.prepare()
+    # the restored context (restart forces in its prepare) goes on as the
+    # uninterrupted one: both agree at the collision step 60
     f.prepare()
-    e.run(20)
-    f.run(20)
+    e.run(30)
+    f.run(30)
     assert_close(f.download_state(), e.download_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)
 
 
@@ -120,6 +119,11 @@ def test_owner_tags_exchange_checkpoint_and_config(tmp_path):
     f = Engine(cfg)
     f.restore(path)
     assert np.array_equal(f.get_owner_tags(), e.get_owner_tags())
+    f.prepare()
+    e.run(30)
+    f.run(30)
+    assert np.array_equal(f.get_owner_tags(), e.get_owner_tags())
+    assert_close(f.download_state(), e.download_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)
     # a context without owner tags refuses the calls; owner tags need the
     # deterministic catalysis of the rotor codes
     plain = Engine(CASES["rot_line"](64))
