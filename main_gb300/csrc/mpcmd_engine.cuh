@@ -7,8 +7,8 @@
 
 namespace mpcmd {
 
-constexpr int TPB = 256;
-constexpr int SHELL_CLASSES = 3;   // pair classes of the shell ordering (k_shell_hist)   // threads per block of the grid-stride kernels
+constexpr int TPB = 256;           // threads per block of the grid-stride kernels
+constexpr int SHELL_CLASSES = 3;   // pair classes of the shell ordering (k_shell_hist)
 
 // Error bits accumulated on the device (mapped to mpcmd_status on the host).
 enum : int {
