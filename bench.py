@@ -35,10 +35,17 @@ WORKLOAD_TEXT = {
     "c1": "collective quasi-2D: 128x128x16 cells with z walls and reactive floor, 2,621,440 solvent, 64 dimers",
     "c2": "Selkov kinetics: 256^3 periodic cells, 167,772,160 solvent (FP32 cell-relative SoA, uint8 species), "
           "512 sphere dimers, six-channel RKMPC",
+    "rot": "rotor grid (rotational_code/2d_array): 64x64x32 cells with z walls, 1,310,720 solvent, "
+           "6x6 anchored dimers with a harmonic z tether",
+    "rot_line": "rotor line (rotational_code/linear_periodic_ci): 256x64x32 cells with z walls, 5,242,880 solvent, "
+                "13 anchored dimers",
+    "rot_owner": "rotor line with owner tags (rotational_code/linear_periodic_no_ci): 256x64x32 cells with z walls, "
+                 "5,242,880 solvent, 13 anchored dimers",
 }
 FALLBACK_HBM = 6800.0
 
-# algorithmic bytes per unit of each kernel kind (FP32 build), see the design doc
+# algorithmic bytes per unit of each kernel kind (FP32 build): the bytes each
+# unit's state must move through DRAM once, whatever the kernel does
 BYTES_PER_PARTICLE_REBUILD = 46      # read flag+cell+offset+velocity (29 B), write cell+offset+flag (17 B)
 BYTES_PER_SHELL_ENTRY = 84           # shell entry written (55 B) and the previous shell entry read (29 B)
 BYTES_PER_SHELL_FORCE = 87           # shell particle read (54 B) and written back (33 B) per MD step
@@ -141,7 +148,7 @@ def ncu_traffic():
 def cpu_sample_config(name, threads):
     from main_gb300 import config
     # same density, dimer density and physics; a box small enough for a bounded CPU sample
-    scale = {"c0": 1.0, "c1": 0.5, "c2": 0.25}[name]
+    scale = {"c0": 1.0, "c1": 0.5, "c2": 0.25, "rot": 0.5, "rot_line": 0.25, "rot_owner": 0.25}[name]
     return config.workload(name, scale=scale, precision=64), scale
 
 
@@ -304,7 +311,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2"])
+    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "rot", "rot_line", "rot_owner"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--dimers", type=int, default=0, help="override the dimer count (profiling cases)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])

@@ -1619,6 +1619,11 @@ __global__ void k_rotor(Dev<T> d, KParams<T> kp, StepArgs a, int mode, int rattl
   if (k >= kp.nd) return;
   const double dt = kp.dtd, Mc = kp.mc, Mn = kp.mn, Dcn = kp.dcn;
   const double hIMc = kp.hIMc, hIMn = kp.hIMn, IIM = kp.IIM;
+  // the FP32 build multiplies by precomputed reciprocals where the reference
+  // divides (FP64 divisions dominate the iteration chain on this part); the
+  // FP64 parity build keeps the reference's operation sequence
+  constexpr bool fast = sizeof(T) == 4;
+  const double iMc = kp.iMc, iMn = kp.iMn, iD2 = kp.iD2, iMcdt = kp.iMcdt, iMndt = kp.iMndt;
   const bool per = kp.geometry == 1;
   const int nwrap = per ? 3 : 2;
   const int s1 = 2 * k, s2 = 2 * k + 1;
@@ -1657,11 +1662,20 @@ __global__ void k_rotor(Dev<T> d, KParams<T> kp, StepArgs a, int mode, int rattl
       for (int c = 0; c < 3; ++c) Vm[c] = 0.5 * (V1[c] + V2[c]);
       if (fabs(Con2diff) < 1.e-8 && fabs(Vm[0]) < 1.e-8 && fabs(Vm[1]) < 1.e-8 && fabs(Vm[2]) < 1.e-8) break;
       if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
-      const double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
-      for (int c = 0; c < 3; ++c) {
-        const double P = -(4.0 * Vm[c] * IIM);
-        V1[c] = V1[c] + O * dd[c] / Mc + 0.5 * P / Mc;
-        V2[c] = V2[c] - O * dd[c] / Mn + 0.5 * P / Mn;
+      if (fast) {
+        const double O = -(0.25 * (IIM * Con2diff) * iD2);
+        for (int c = 0; c < 3; ++c) {
+          const double hP = -(2.0 * Vm[c] * IIM);
+          V1[c] = V1[c] + (O * dd[c] + hP) * iMc;
+          V2[c] = V2[c] + (hP - O * dd[c]) * iMn;
+        }
+      } else {
+        const double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
+        for (int c = 0; c < 3; ++c) {
+          const double P = -(4.0 * Vm[c] * IIM);
+          V1[c] = V1[c] + O * dd[c] / Mc + 0.5 * P / Mc;
+          V2[c] = V2[c] - O * dd[c] / Mn + 0.5 * P / Mn;
+        }
       }
       acc++;
     }
@@ -1701,20 +1715,41 @@ __global__ void k_rotor(Dev<T> d, KParams<T> kp, StepArgs a, int mode, int rattl
       const double Con1diff = (dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) - Dcn * Dcn;
       if (fabs(Con1diff) < 1.e-6 && fabs(D[0]) < 1.e-6 && fabs(D[1]) < 1.e-6 && fabs(D[2]) < 1.e-6) break;
       if (acc == rattle_max) { atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
-      const double G = -(0.25 * Con1diff * IIM / (dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2]));
-      double H[3];
-      for (int c = 0; c < 3; ++c) H[c] = -(4.0 * IIM * D[c]);
-      for (int c = 0; c < 3; ++c) {
-        X1[c] = pr1[c] + Q1[c] * dt + G * dP[c] / Mc + 0.5 * H[c] / Mc;
-        X2[c] = pr2[c] + Q2[c] * dt - G * dP[c] / Mn + 0.5 * H[c] / Mn;
-      }
-      for (int c = 0; c < 3; ++c) {
-        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
-        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
-      }
-      for (int c = 0; c < 3; ++c) {
-        Q1[c] = Q1[c] + G * dP[c] / (Mc * dt) + 0.5 * H[c] / (Mc * dt);
-        Q2[c] = Q2[c] - G * dP[c] / (Mn * dt) + 0.5 * H[c] / (Mn * dt);
+      const double den = dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2];
+      if (fast) {
+        // a float reciprocal refined twice replaces the division (the
+        // iteration converges to the tolerance whatever G's last bits are)
+        double r = (double)__frcp_rn((float)den);
+        r = r * (2.0 - den * r);
+        r = r * (2.0 - den * r);
+        const double G = -(0.25 * Con1diff * IIM) * r;
+        for (int c = 0; c < 3; ++c) {
+          const double hH = -(2.0 * IIM * D[c]);
+          const double u1 = G * dP[c] + hH, u2 = hH - G * dP[c];
+          X1[c] = pr1[c] + Q1[c] * dt + u1 * iMc;
+          X2[c] = pr2[c] + Q2[c] * dt + u2 * iMn;
+          const double L = kp.Ld[c];
+          if (X1[c] >= L) X1[c] -= L; else if (X1[c] < 0.0) X1[c] += L;
+          if (X2[c] >= L) X2[c] -= L; else if (X2[c] < 0.0) X2[c] += L;
+          Q1[c] = Q1[c] + u1 * iMcdt;
+          Q2[c] = Q2[c] + u2 * iMndt;
+        }
+      } else {
+        const double G = -(0.25 * Con1diff * IIM / den);
+        double H[3];
+        for (int c = 0; c < 3; ++c) H[c] = -(4.0 * IIM * D[c]);
+        for (int c = 0; c < 3; ++c) {
+          X1[c] = pr1[c] + Q1[c] * dt + G * dP[c] / Mc + 0.5 * H[c] / Mc;
+          X2[c] = pr2[c] + Q2[c] * dt - G * dP[c] / Mn + 0.5 * H[c] / Mn;
+        }
+        for (int c = 0; c < 3; ++c) {
+          X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+          X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+        }
+        for (int c = 0; c < 3; ++c) {
+          Q1[c] = Q1[c] + G * dP[c] / (Mc * dt) + 0.5 * H[c] / (Mc * dt);
+          Q2[c] = Q2[c] - G * dP[c] / (Mn * dt) + 0.5 * H[c] / (Mn * dt);
+        }
       }
       acc++;
     }
@@ -1895,11 +1930,147 @@ void Launch<T>::sphere_totals(const Dev<T>& d, const KParams<T>& kp, double w3, 
   LAUNCH_COUNT();
 }
 
+// The FP32 build's rotor step (k_rotor's fast path) with the three Cartesian
+// components of a rotor on three lanes of a 4-lane group, the constraint dot
+// products summed across the group and the convergence tests taken over it;
+// the fourth lane holds zeros and the energy.  As for k_dimer_split, the
+// per-rotor chain of FP64 instructions sets the time, and the split shortens
+// it about threefold.
+template <typename T>
+__global__ void k_rotor_split(Dev<T> d, KParams<T> kp, StepArgs a, int mode, int rattle_max) {
+  if (d.ctr->abort_step) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = t >> 2, c = t & 3;
+  const unsigned gmask = 0xFu << (threadIdx.x & 28);   // this group's four lanes
+  const bool live = k < kp.nd;        // the whole 4-lane group agrees
+  const int kk = live ? k : 0;
+  const bool comp = c < 3;
+  const double dt = kp.dtd, Dcn = kp.dcn;
+  const double hIMc = kp.hIMc, hIMn = kp.hIMn, IIM = kp.IIM;
+  const double iMc = kp.iMc, iMn = kp.iMn, iD2 = kp.iD2, iMcdt = kp.iMcdt, iMndt = kp.iMndt;
+  const bool per = kp.geometry == 1;
+  const int cc = comp ? c : 0;
+  const bool mi = comp && (c < 2 || per);   // minimum image on this axis
+  const double L = kp.Ld[cc];
+  const int s1 = 2 * kk, s2 = 2 * kk + 1;
+  double X1 = 0, X2 = 0, V1 = 0, V2 = 0, F1 = 0, F2 = 0, Q1 = 0, Q2 = 0, A = 0;
+  if (live && comp) {
+    X1 = d.dpos[3 * s1 + c]; X2 = d.dpos[3 * s2 + c];
+    V1 = d.dvel[3 * s1 + c]; V2 = d.dvel[3 * s2 + c];
+    F1 = d.dfrc[3 * s1 + c]; F2 = d.dfrc[3 * s2 + c];
+    Q1 = d.dq[3 * s1 + c]; Q2 = d.dq[3 * s2 + c];
+    A = d.anchor[3 * kk + c];
+  }
+  unsigned long long iters = 0;
+  if (mode & 1) {
+    double fw1 = 0., pw1 = 0., fw2 = 0., pw2 = 0.;
+    if (live && c == 2) {
+      harmonic_tether(X1, kp.tether_z, kp.tether_k, fw1, pw1);
+      harmonic_tether(X2, kp.tether_z, kp.tether_k, fw2, pw2);
+    }
+    // the tether energies travel from the z lane to the energy lane
+    const int zl = (threadIdx.x & 31 & ~3) | 2;
+    const double p1 = __shfl_sync(gmask, pw1, zl), p2 = __shfl_sync(gmask, pw2, zl);
+    if (live) {
+      const int q = comp ? c : 3;
+      const double a1 = d.facc[4 * s1 + q], a2 = d.facc[4 * s2 + q];
+      d.facc[4 * s1 + q] = 0.; d.facc[4 * s2 + q] = 0.;
+      if (comp) {
+        F1 = a1 + (c == 2 ? fw1 : 0.);
+        F2 = a2 + (c == 2 ? fw2 : 0.);
+      } else {
+        d.dpot[kk] = (a1 + p1) + (a2 + p2);
+      }
+    }
+    if (comp) { V1 = Q1 + hIMc * F1; V2 = Q2 + hIMn * F2; }
+    int acc = 0;
+    for (;;) {
+      double dd = X1 - X2;
+      if (mi) dd = dmin_image(dd, L);
+      if (!comp) dd = 0.;
+      const double Con2diff = group4_sum(gmask, (V1 - V2) * dd);
+      const double Vm = 0.5 * (V1 + V2);
+      const bool vm_ok = __all_sync(gmask, !comp || fabs(Vm) < 1.e-8);
+      if (!live || (fabs(Con2diff) < 1.e-8 && vm_ok)) break;
+      if (acc == rattle_max) { if (c == 0) atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      const double O = -(0.25 * (IIM * Con2diff) * iD2);
+      const double hP = -(2.0 * Vm * IIM);
+      V1 = V1 + (O * dd + hP) * iMc;
+      V2 = V2 + (hP - O * dd) * iMn;
+      acc++;
+    }
+    iters += acc;
+    if (live && comp) {
+      d.dvel[3 * s1 + c] = V1; d.dvel[3 * s2 + c] = V2;
+      d.dfrc[3 * s1 + c] = F1; d.dfrc[3 * s2 + c] = F2;
+    }
+  }
+  if (mode & 2) {
+    const double pr1 = X1, pr2 = X2;
+    double dP = X1 - X2;
+    if (mi) dP = dmin_image(dP, L);
+    if (!comp) dP = 0.;
+    Q1 = V1 + hIMc * F1; Q2 = V2 + hIMn * F2;
+    X1 = X1 + dt * Q1; X2 = X2 + dt * Q2;
+    if (comp && (c < 2 || per)) {
+      if (X1 >= L) X1 -= L; else if (X1 < 0.0) X1 += L;
+      if (X2 >= L) X2 -= L; else if (X2 < 0.0) X2 += L;
+    }
+    int acc = 0;
+    for (;;) {
+      double dd = X1 - X2;
+      if (mi) dd = dmin_image(dd, L);
+      if (!comp) dd = 0.;
+      double m = 0.5 * (X1 + X2);
+      if (c < 2) {
+        if (m >= L) m = m - L;
+        else if (m < 0.) m = m + L;
+      }
+      const double D = m - A;
+      const double Con1diff = group4_sum(gmask, dd * dd) - Dcn * Dcn;
+      const bool d_ok = __all_sync(gmask, !comp || fabs(D) < 1.e-6);
+      if (!live || (fabs(Con1diff) < 1.e-6 && d_ok)) break;
+      if (acc == rattle_max) { if (c == 0) atomicOr(&d.ctr->status, DEV_ERR_RATTLE); break; }
+      const double den = group4_sum(gmask, dd * dP);
+      double r = (double)__frcp_rn((float)den);
+      r = r * (2.0 - den * r);
+      r = r * (2.0 - den * r);
+      const double G = -(0.25 * Con1diff * IIM) * r;
+      const double hH = -(2.0 * IIM * D);
+      const double u1 = G * dP + hH, u2 = hH - G * dP;
+      X1 = pr1 + Q1 * dt + u1 * iMc;
+      X2 = pr2 + Q2 * dt + u2 * iMn;
+      if (comp) {   // every axis wraps inside the iteration (2d_array/evolve_mod.f95:365-369)
+        if (X1 >= L) X1 -= L; else if (X1 < 0.0) X1 += L;
+        if (X2 >= L) X2 -= L; else if (X2 < 0.0) X2 += L;
+      }
+      Q1 = Q1 + u1 * iMcdt;
+      Q2 = Q2 + u2 * iMndt;
+      acc++;
+    }
+    iters += acc;
+    if (live && comp) {
+      d.dpos[3 * s1 + c] = X1; d.dpos[3 * s2 + c] = X2;
+      d.dq[3 * s1 + c] = Q1; d.dq[3 * s2 + c] = Q2;
+      const double f1 = floor(X1), f2 = floor(X2);
+      SphereRel<T>& r1 = d.srel[s1];
+      SphereRel<T>& r2 = d.srel[s2];
+      if (c == 0) { r1.cx = (int)f1; r1.ox = (T)(X1 - f1); r2.cx = (int)f2; r2.ox = (T)(X2 - f2); }
+      else if (c == 1) { r1.cy = (int)f1; r1.oy = (T)(X1 - f1); r2.cy = (int)f2; r2.oy = (T)(X2 - f2); }
+      else { r1.cz = (int)f1; r1.oz = (T)(X1 - f1); r2.cz = (int)f2; r2.oz = (T)(X2 - f2); }
+    }
+  }
+  if (live && c == 0 && iters) atomicAdd(&d.ctr->rattle_iters, iters);
+}
+
 template <typename T>
 void Launch<T>::dimer(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, int mode, double w3,
                       int rattle_max, cudaStream_t st) {
   if (kp.nd == 0) return;
-  if (kp.rotor) {
+  if (kp.rotor && sizeof(T) == 4) {
+    const int threads = 4 * kp.nd;
+    k_rotor_split<T><<<(threads + 31) / 32, 32, 0, st>>>(d, kp, a, mode, rattle_max);
+  } else if (kp.rotor) {
     k_rotor<T><<<(kp.nd + 63) / 64, 64, 0, st>>>(d, kp, a, mode, rattle_max);
   } else if (sizeof(T) == 4) {
     // four lanes per dimer, one 32-lane block per eight dimers (spread over the SMs)
