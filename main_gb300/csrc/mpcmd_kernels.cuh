@@ -2239,7 +2239,7 @@ static __device__ int selkov_channel_fp32(const float* kf, float tau, int nF, in
 // RMPC_SelkovDimer.f90:127-324) and the reset of the accumulators.
 // what bit 0: collision tables, bit 1: reaction.
 template <typename T>
-__global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs a, int what) {
+__global__ void __launch_bounds__(TPB, 6) k_cells(Dev<T> d, KParams<T> kp, StepArgs a, int what) {
   if (d.ctr->abort_step) return;
   const int64_t nmax = kp.ncell_shift > kp.ncell ? kp.ncell_shift : kp.ncell;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -2318,8 +2318,10 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
           if (fire && fk[1] != 0xFFFFFFFFu) relabel_key(d, fk[1], 0);
         }
       } else if (kp.kinetics == 2 && !d.affected[c]) {
-        const int tgt[7] = {-1, 3, 0, 0, 1, 1, 3};
-        const int code[7] = {-1, 0, 3, 1, 0, 3, 1};
+        // channel 1..6 -> species relabelled (target) and its new code, one
+        // nibble per channel (RMPC_SelkovDimer.f90:132-321): targets 3 0 0 1 1 3,
+        // codes 0 3 1 0 3 1 (register constants instead of a local table)
+        const unsigned tgt_nib = 0x3110030u, code_nib = 0x1301300u;
         int nF = cnt & 255u, nG = (cnt >> 8) & 255u, nI = (cnt >> 24) & 255u;
         int ch = -1;
         if (sizeof(T) == 4) {
@@ -2334,8 +2336,8 @@ __global__ void __launch_bounds__(TPB) k_cells(Dev<T> d, KParams<T> kp, StepArgs
           ch = selkov_channel_fp64(kp.k, kp.tau, nF, nG, nI, x1, x2);
         }
         if (ch > 0) {
-          const uint32_t key = fk[tgt[ch]];
-          if (key != 0xFFFFFFFFu) relabel_key(d, key, code[ch]);
+          const uint32_t key = fk[(tgt_nib >> (4 * ch)) & 0xFu];
+          if (key != 0xFFFFFFFFu) relabel_key(d, key, (int)((code_nib >> (4 * ch)) & 0xFu));
         }
       }
       d.dcnt[c] = 0u;
