@@ -681,7 +681,9 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
         int np = 0;
         bool nonbulk = false;
         T min_gap = (T)1e30;
-        uint16_t sph[PAIRMAX];
+        // sphere ids of the pairs, 16 bits per slot packed in two registers
+        // (slots 0-3 and 4-7; 0xFFFF = empty), no indexed local array
+        unsigned long long slo = ~0ull, shi = ~0ull;
         if (kp.ns > 0) {
           int bin = bin_of(kp.lx, kp.ly, kp.nbx, kp.nby, cell);
           bool okb = chk(bin >= 0 && bin < kp.nbx * kp.nby * kp.nbz, d.ctr, 110, (long long)cell);
@@ -695,7 +697,12 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
             T dx, dy, dz;
             T d2 = sep2(kp, cell, ox, oy, oz, sr, dx, dy, dz);
             if (d2 <= kp.full2[s & 1]) {
-              if (np < PAIRMAX) sph[np] = (uint16_t)s;
+              if (np < PAIRMAX) {
+                const int sh = 16 * (np & 3);
+                const unsigned long long m = ~(0xFFFFull << sh), v = (unsigned long long)(uint16_t)s << sh;
+                if (np < 4) slo = (slo & m) | v;
+                else shi = (shi & m) | v;
+              }
               np++;
               if (d2 <= kp.cut2[s & 1]) nonbulk = true;
               if (a.horizon > 0) {
@@ -729,12 +736,9 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
             d.sh2.flag[j] = sp | FLAG_INLIST;
             d.sh2.nonbulk[j] = nonbulk ? 1 : 0;
             d.sh2.np[j] = (uint8_t)np;
-            uint16_t v[PAIRMAX];
-#pragma unroll
-            for (int q = 0; q < PAIRMAX; ++q) v[q] = q < np ? sph[q] : (uint16_t)0xFFFF;
             uint4 packed;
-            packed.x = v[0] | ((uint32_t)v[1] << 16); packed.y = v[2] | ((uint32_t)v[3] << 16);
-            packed.z = v[4] | ((uint32_t)v[5] << 16); packed.w = v[6] | ((uint32_t)v[7] << 16);
+            packed.x = (uint32_t)slo; packed.y = (uint32_t)(slo >> 32);
+            packed.z = (uint32_t)shi; packed.w = (uint32_t)(shi >> 32);
             *reinterpret_cast<uint4*>(d.sh2.sph + (size_t)j * PAIRMAX) = packed;
             d.p.cell[i] = j;
             d.p.flag[i] = sp | FLAG_INLIST | FLAG_HOME_SHELL;
@@ -1208,7 +1212,9 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
             (uint16_t)(packed.y >> 16), (uint16_t)(packed.z & 0xFFFFu), (uint16_t)(packed.z >> 16),
             (uint16_t)(packed.w & 0xFFFFu), (uint16_t)(packed.w >> 16)};
         T min_gap = (T)1e30;
-        for (int q = 0; q < np; ++q) {
+#pragma unroll
+        for (int q = 0; q < PAIRMAX; ++q) {
+          if (q >= np) break;
           const int s = ids[q];
           if (!chk(s < kp.ns, d.ctr, 121, s)) { min_gap = (T)-1; break; }
           T dx, dy, dz;
