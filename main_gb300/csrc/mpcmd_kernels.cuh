@@ -983,7 +983,7 @@ void Launch<T>::finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const St
 // (forces_mod.f95:144-210) of the current sphere positions.
 // OWN: the owner-tag form (a template flag: the common form keeps no tag state)
 template <typename T, bool OWN>
-__global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs a) {
+__global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d, KParams<T> kp, StepArgs a) {
   if (d.ctr->abort_step) return;
   if (!a.rebuilt) {
     // max_solvent_dist > threshold, compared on the double bits (both >= 0)
@@ -1076,10 +1076,17 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
     // owner tag (type_B) of the particle, with owner_tags
     uint32_t own = 0, own0 = 0;
     if (OWN && act) own = own0 = d.owner[idx];
+    // The FP32 build sums an entry's pair forces for its two half kicks (and
+    // stores the per-pair forces kept across a step boundary inside the
+    // loop), which frees the per-slot registers; the FP64 parity build kicks
+    // pair by pair in the reference's order (evolve_mod.f95:225-250, :645-670).
+    constexpr bool SUMK = sizeof(T) == 4;
+    const bool keep_pf = !(a.advance && !a.mpc);
     T fpx[PAIRMAX], fpy[PAIRMAX], fpz[PAIRMAX];
+    T Fx = (T)0, Fy = (T)0, Fz = (T)0;
 #pragma unroll
     for (int q = 0; q < PAIRMAX; ++q) {
-      fpx[q] = fpy[q] = fpz[q] = (T)0;
+      if (!SUMK) fpx[q] = fpy[q] = fpz[q] = (T)0;
       if (!__any_sync(0xffffffffu, q < np)) break;
       int s = (q < np) ? (int)sphl[q] : -1;
       T fx = 0, fy = 0, fz = 0, u = 0;
@@ -1114,15 +1121,27 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
           s = -1;   // in the skin only: no contribution
         }
       }
-      fpx[q] = fx; fpy[q] = fy; fpz[q] = fz;
+      if (SUMK) {
+        Fx += fx; Fy += fy; Fz += fz;
+        if (keep_pf && q < np) {
+          const size_t bq = ((size_t)j * PAIRMAX + q) * 3;
+          d.sh.pf[bq] = fx; d.sh.pf[bq + 1] = fy; d.sh.pf[bq + 2] = fz;
+        }
+      } else {
+        fpx[q] = fx; fpy[q] = fy; fpz[q] = fz;
+      }
       warp_sphere_add(d.facc, s, -fx, -fy, -fz, u);
     }
     if (act) {
       const T h2 = kp.hIM[fl & FLAG_SPECIES];
+      if (SUMK) {
+        if (!a.forces_only) { vx = vx + h2 * Fx; vy = vy + h2 * Fy; vz = vz + h2 * Fz; }
+      } else {
 #pragma unroll
-      for (int q = 0; q < PAIRMAX; ++q) {
-        if (q >= np || a.forces_only) break;
-        vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
+        for (int q = 0; q < PAIRMAX; ++q) {
+          if (q >= np || a.forces_only) break;
+          vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
+        }
       }
       if (a.mpc) {
         uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
@@ -1136,10 +1155,14 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
         }
       }
       if (a.advance && !a.mpc) {
+        if (SUMK) {
+          vx = vx + h2 * Fx; vy = vy + h2 * Fy; vz = vz + h2 * Fz;
+        } else {
 #pragma unroll
-        for (int q = 0; q < PAIRMAX; ++q) {
-          if (q >= np) break;
-          vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
+          for (int q = 0; q < PAIRMAX; ++q) {
+            if (q >= np) break;
+            vx = vx + h2 * fpx[q]; vy = vy + h2 * fpy[q]; vz = vz + h2 * fpz[q];
+          }
         }
         stream_one(kp, d.react_box, cell, ox, oy, oz, vx, vy, vz, fl, false, 1);
         T msd = msd0 + (vx * vx + vy * vy + vz * vz) * (kp.dt * kp.dt);
@@ -1147,7 +1170,7 @@ __global__ void __launch_bounds__(TPB) k_force(Dev<T> d, KParams<T> kp, StepArgs
         msdmax = msd > msdmax ? msd : msdmax;
         d.sh.cell[j] = cell;
         d.sh.ox[j] = ox; d.sh.oy[j] = oy; d.sh.oz[j] = oz;
-      } else {
+      } else if (!SUMK) {
 #pragma unroll
         for (int q = 0; q < PAIRMAX; ++q) {
           if (q >= np) break;
