@@ -152,13 +152,17 @@ def cpu_sample_config(name, threads):
     return config.workload(name, scale=scale, precision=64), scale
 
 
-def cpu_baseline(name, cycles_max=5, seconds=12.0):
-    """FP64 oracle (OpenMP, all host cores) on a bounded sample of the workload."""
+def cpu_baseline(name, cycles_max=5, seconds=12.0, cell_lists=False):
+    """FP64 oracle (OpenMP, all host cores) on a bounded sample of the workload.
+    cell_lists: the pair search through cell bins instead of the reference's
+    all-pairs loop (same lists, same results; a faster CPU for comparison)."""
     from oracle.oracle import Oracle
     import oracle.oracle as O
     threads = os.cpu_count() or 1
     cfg, scale = cpu_sample_config(name, threads)
     o = Oracle(cfg, threads=threads)
+    if cell_lists:
+        o.set_list_mode(O.LISTS_CELLS)
     o.initial()
     o.prepare()
     S = cfg["mpc_every"]
@@ -360,6 +364,10 @@ def main():
     if rk == 0 and ws == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, seconds=args.cpu_seconds)
         cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # the same sample with the pair search through cell bins (same lists,
+        # same trajectory), the faster of the two CPU loop structures
+        cc = cpu_baseline(args.workload, seconds=args.cpu_seconds, cell_lists=True)
+        cb["cell_list_value"] = cc["value"]
     if rk == 0:
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,

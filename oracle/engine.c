@@ -397,11 +397,95 @@ int orc_sort(orc_t* o) {
 
 /* --------------------------------------------------------- neighbours -- */
 /* neighbour_list_mod.f95:6-59 for every sphere, then :63-184 inout split. */
+int orc_set_list_mode(orc_t* o, int mode) {
+  if (mode != ORC_LISTS_ALL_PAIRS && mode != ORC_LISTS_CELLS) return ORC_ERR_CONFIG;
+  o->list_mode = mode;
+  return ORC_OK;
+}
+
+/* The lists of orc_rebuild_lists through cell bins: the particles are binned
+ * by cell once, each sphere visits the cells its list radius reaches and
+ * sorts what it finds by index, and the inside list is the particles found
+ * by any sphere, in index order: the same lists, in the same order, as the
+ * all-pairs search, without its N x spheres distance tests. */
+static int cmp_i64(const void* a, const void* b) {
+  const int64_t x = *(const int64_t*)a, y = *(const int64_t*)b;
+  return (x > y) - (x < y);
+}
+
+static int rebuild_lists_cells(orc_t* o, double fullC2, double fullN2) {
+  const int64_t n = o->nt, C = o->ncell;
+  const int lx = o->p.lx, ly = o->p.ly, lz = o->p.lz;
+  const int periodic = o->p.geometry == ORC_GEOM_PERIODIC;
+  int64_t* start = calloc(C + 1, 8);
+  int64_t* fill = malloc((C + 1) * 8);
+  int64_t* byc = malloc(n * 8);
+  uint8_t* in = calloc(n, 1);
+  if (!start || !fill || !byc || !in) {
+    free(start); free(fill); free(byc); free(in);
+    return o->status = ORC_ERR_ALLOC;
+  }
+  for (int64_t i = 0; i < n; ++i) start[clamp_cell(o, cell_of(o, o->x[i], o->y[i], o->z[i])) + 1]++;
+  for (int64_t c = 0; c < C; ++c) start[c + 1] += start[c];
+  memcpy(fill, start, (C + 1) * 8);
+  for (int64_t i = 0; i < n; ++i) byc[fill[clamp_cell(o, cell_of(o, o->x[i], o->y[i], o->z[i]))]++] = i;
+  int overflow = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(|:overflow)
+  for (int s = 0; s < o->ns; ++s) {
+    const double full2 = (s % 2 == 0) ? fullC2 : fullN2, R = sqrt(full2);
+    const double* P = o->dpos + 3 * s;
+    int64_t cntl = 0;
+    int64_t* list = o->nb + (int64_t)s * o->maxnb;
+    const int x0 = (int)floor(P[0] - R) - 1, x1 = (int)floor(P[0] + R) + 1;
+    const int y0 = (int)floor(P[1] - R) - 1, y1 = (int)floor(P[1] + R) + 1;
+    int z0 = (int)floor(P[2] - R) - 1, z1 = (int)floor(P[2] + R) + 1;
+    if (!periodic) { if (z0 < 0) z0 = 0; if (z1 > lz - 1) z1 = lz - 1; }
+    /* a range as wide as the box visits every cell of that axis once */
+    int xa = x0, xb = x1, ya = y0, yb = y1;
+    if (xb - xa + 1 >= lx) { xa = 0; xb = lx - 1; }
+    if (yb - ya + 1 >= ly) { ya = 0; yb = ly - 1; }
+    if (periodic && z1 - z0 + 1 >= lz) { z0 = 0; z1 = lz - 1; }
+    for (int cz = z0; cz <= z1; ++cz)
+      for (int cy = ya; cy <= yb; ++cy)
+        for (int cx = xa; cx <= xb; ++cx) {
+          const int wx = ((cx % lx) + lx) % lx, wy = ((cy % ly) + ly) % ly;
+          const int wz = periodic ? ((cz % lz) + lz) % lz : cz;
+          const int64_t c = wx + (int64_t)lx * (wy + (int64_t)ly * wz);
+          for (int64_t q = start[c]; q < start[c + 1]; ++q) {
+            const int64_t i = byc[q];
+            double dR[3];
+            if (sol_sphere_d(o, i, s, dR) <= full2) {
+              if (cntl < o->maxnb) list[cntl] = i;
+              else overflow = 1;
+              cntl++;
+            }
+          }
+        }
+    const int64_t m = cntl < o->maxnb ? cntl : o->maxnb;
+    /* index order, as the all-pairs loop finds them */
+    qsort(list, (size_t)m, sizeof(int64_t), cmp_i64);
+    o->nbnum[s] = m;
+  }
+  if (overflow) o->status = ORC_ERR_NEIGHBOUR_OVERFLOW;
+  for (int s = 0; s < o->ns; ++s)
+    for (int64_t q = 0; q < o->nbnum[s]; ++q) in[o->nb[(int64_t)s * o->maxnb + q]] = 1;
+  int64_t nin = 0, nout = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (in[i]) o->in_list[nin++] = i;
+    else o->out_list[nout++] = i;
+  }
+  o->n_in = nin;
+  o->n_out = nout;
+  free(start); free(fill); free(byc); free(in);
+  return o->status;
+}
+
 int orc_rebuild_lists(orc_t* o) {
   const double cut = pow(2.0, 1.0 / 6.0);
   const double cutC = o->p.rc * cut, cutN = o->p.rn * cut;
   const double fullC2 = (cutC + o->p.skin) * (cutC + o->p.skin);
   const double fullN2 = (cutN + o->p.skin) * (cutN + o->p.skin);
+  if (o->list_mode == ORC_LISTS_CELLS) return rebuild_lists_cells(o, fullC2, fullN2);
   const int64_t n = o->nt;
   int overflow = 0;
 #pragma omp parallel for schedule(static) reduction(|:overflow)

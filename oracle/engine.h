@@ -39,6 +39,7 @@ struct orc {
   int32_t* react_box;         /* [lx*ly]                                           */
   int32_t* order;             /* cell visiting order of the sort, NULL = row-major  */
   int rng_mode, mt_kind;
+  int list_mode;              /* ORC_LISTS_*: how orc_rebuild_lists finds the pairs  */
   uint32_t mt[624];
   int32_t mti;
   int status;

@@ -30,6 +30,10 @@ enum { ORC_KIN_NONE = 0, ORC_KIN_SIMPLE = 1, ORC_KIN_SELKOV = 2 };
 enum { ORC_EXCL_PARTICLE = 0, ORC_EXCL_CELLS = 1 };
 enum { ORC_CAT_DETERMINISTIC = 0, ORC_CAT_PROBABILISTIC = 1 };
 enum { ORC_RNG_CONTRACT = 0, ORC_RNG_MT = 1 };
+/* Pair search of orc_rebuild_lists: every particle against every sphere
+ * (neighbour_list_mod.f95, the default), or through cell bins (the same
+ * lists in the same order; a faster CPU baseline for comparison). */
+enum { ORC_LISTS_ALL_PAIRS = 0, ORC_LISTS_CELLS = 1 };
 /* rotational_code variants: ROTOR anchors every dimer's midpoint
  * (rotational_code/2d_array); dimer layouts of the initial placement. */
 enum { ORC_VARIANT_MOTOR = 0, ORC_VARIANT_ROTOR = 1 };
@@ -112,6 +116,7 @@ int orc_set_threads(int n);
 
 /* RNG selection: contract (Philox, default) or MT19937 serial reference order. */
 int orc_set_rng(orc_t* o, int mode, uint32_t mt_seed);
+int orc_set_list_mode(orc_t* o, int mode);
 
 /* State exchange.  Dimer arrays hold n_dimers*2 spheres (s = 2k+i) x 3 comps. */
 int orc_set_state(orc_t* o, const double* x, const double* y, const double* z,

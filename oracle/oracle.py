@@ -44,6 +44,7 @@ class OrcObs(C.Structure):
 
 
 RNG_CONTRACT, RNG_MT = 0, 1
+LISTS_ALL_PAIRS, LISTS_CELLS = 0, 1
 _lib = None
 
 
@@ -63,6 +64,7 @@ def lib():
             "orc_status": (C.c_int, [P]),
             "orc_set_threads": (C.c_int, [C.c_int]),
             "orc_set_rng": (C.c_int, [P, C.c_int, C.c_uint32]),
+            "orc_set_list_mode": (C.c_int, [P, C.c_int]),
             "orc_set_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
             "orc_get_state": (C.c_int, [P, dp, dp, dp, dp, dp, dp, ip, dp, dp, dp]),
             "orc_restart_forces": (C.c_int, [P]),
@@ -195,6 +197,9 @@ class Oracle:
 
     def set_rng(self, mode, mt_seed=0):
         lib().orc_set_rng(self.h, mode, mt_seed)
+
+    def set_list_mode(self, mode):
+        self._check(lib().orc_set_list_mode(self.h, mode), "set_list_mode")
 
     def set_state(self, st):
         f = lambda k: np.ascontiguousarray(st[k], dtype=np.float64)

@@ -275,3 +275,24 @@ def test_selkov_driver_matches_hybrid_driver():
         assert np.max(np.abs(sa[k] - sb[k])) < 1e-9, k
     assert (sa["flag"] == sb["flag"]).mean() > 0.999
     assert np.max(np.abs(sa["dpos"] - sb["dpos"])) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["c0", "c1"])
+def test_cell_list_search_gives_the_same_run(name):
+    # the cell-binned pair search (a CPU baseline for comparison) finds the
+    # same lists in the same order as neighbour_list_mod.f95's all-pairs loop
+    import oracle.oracle as O
+    cfg = small(name)
+    a = Oracle(cfg, threads=4)
+    a.initial()
+    st = a.get_state()
+    b = Oracle(cfg, threads=4)
+    b.set_state(st)
+    b.set_list_mode(O.LISTS_CELLS)
+    a.prepare()
+    b.prepare()
+    a.run(60)
+    b.run(60)
+    sa, sb = a.get_state(), b.get_state()
+    for k in ("x", "y", "z", "vx", "vy", "vz", "flag", "dpos", "dvel"):
+        assert np.array_equal(sa[k], sb[k]), k
