@@ -223,3 +223,25 @@ def test_owner_tags_follow_the_particles():
     assert np.all((own[b] >= 1) & (own[b] <= cfg["n_dimers"]))
     # every motor has made some of them
     assert set(np.unique(own[b])) == set(range(1, cfg["n_dimers"] + 1))
+
+
+def test_rotational_deck_mapping(tmp_path):
+    # a deck in the layout of rotational_code/2d_array/input.txt (one value per
+    # line, a comment after it) maps to the rotor configuration of
+    # main_rotation.f95:53-110
+    vals = ["6048421", "2000", "10.", "0.", "32.", "32.", "16.", "0", "2", "3", "1.0", "1.0", "2.0", "2.0",
+            "5.0", "0.1", "0.1", "0.1", "1.0", "1000.0", "1.0", "1.0", "0.0", "0.2", "0.7", "1.0",
+            "1.5707963267948966192", "0.005", "0.1", "10000", "0.001", "100", "100", "100", "100"]
+    deck = tmp_path / "input.txt"
+    deck.write_text("".join("%s\t\tvalue %d\n" % (v, i) for i, v in enumerate(vals)))
+    c = config.rotational_config(config.read_rotational_input(str(deck)))
+    assert (c["lx"], c["ly"], c["lz"], c["n_dimers"], c["layout_rows"], c["layout_cols"]) == (32, 32, 16, 6, 2, 3)
+    assert c["variant"] == config.VARIANT_ROTOR and c["layout"] == config.LAYOUT_GRID
+    assert c["tether_k"] == 1000.0 and c["tether_z"] == 3.0 and c["mpc_every"] == 20
+    assert c["n_solvent"] == math.floor(10.0 * 32 * 32 * 16) and c["init_count"][1] == 0
+    assert c["k"][0] == 0.001 and c["eps_n"][:2] == [0.1, 1.0] and c["react_box_type"] == 0
+    # the oracle takes it: the layout lands in the box at the tether plane
+    o = O.Oracle(dict(c, n_solvent=2048, init_count=[2048, 0, 0, 0]), threads=2)
+    o.initial()
+    d = o.get_state()["dpos"]
+    assert np.all((d[:, 0] > 0) & (d[:, 0] < 32) & (d[:, 1] > 0) & (d[:, 1] < 32)) and np.all(d[:, 2] == 3.0)
