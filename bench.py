@@ -152,14 +152,20 @@ def cpu_sample_config(name, threads):
     return config.workload(name, scale=scale, precision=64), scale
 
 
-def cpu_baseline(name, cycles_max=5, seconds=12.0, cell_lists=False):
+def cpu_baseline(name, cycles_max=5, seconds=12.0, cell_lists=False, full=False):
     """FP64 oracle (OpenMP, all host cores) on a bounded sample of the workload.
     cell_lists: the pair search through cell bins instead of the reference's
-    all-pairs loop (same lists, same results; a faster CPU for comparison)."""
+    all-pairs loop (same lists, same results; a faster CPU for comparison).
+    full: the workload at its full size instead of the sample (one timed
+    collision period after the untimed initial placement and prepare)."""
     from oracle.oracle import Oracle
     import oracle.oracle as O
+    from main_gb300 import config
     threads = os.cpu_count() or 1
-    cfg, scale = cpu_sample_config(name, threads)
+    if full:
+        cfg, scale = config.workload(name, precision=64), 1.0
+    else:
+        cfg, scale = cpu_sample_config(name, threads)
     o = Oracle(cfg, threads=threads)
     if cell_lists:
         o.set_list_mode(O.LISTS_CELLS)
@@ -175,11 +181,12 @@ def cpu_baseline(name, cycles_max=5, seconds=12.0, cell_lists=False):
             break
     dt = time.perf_counter() - t0
     value = cfg["n_solvent"] * S * cycles / dt
-    sample = ("%s scaled by %.2f per edge: %dx%dx%d cells, %d solvent, %d dimers; %d collision period(s) of %d MD "
-              "steps after prepare" % (name, scale, cfg["lx"], cfg["ly"], cfg["lz"], cfg["n_solvent"],
-                                       cfg["n_dimers"], cycles, S, ))
+    box = "%dx%dx%d cells, %d solvent, %d dimers" % (cfg["lx"], cfg["ly"], cfg["lz"], cfg["n_solvent"],
+                                                      cfg["n_dimers"])
+    sample = ("%s scaled by %.2f per edge: %s; %d collision period(s) of %d MD steps after prepare"
+              % (name, scale, box, cycles, S))
     return {"value": value, "unit": UNIT, "cores": O.lib().orc_set_threads(0), "kind": "port",
-            "sample": sample, "seconds": dt}
+            "sample": sample, "seconds": dt, "box": box}
 
 
 def pinned_state(n, ns):
@@ -279,6 +286,23 @@ def gpu_arm(args, ws, rk, lr, dist):
         "share_of_timed": {k: round(prof[k][0] / sum(v[0] for v in prof.values()), 4) for k in kinds if prof[k][1]},
     }
 
+    # mean period over one whole sort cycle of the workload (its sort_every MD
+    # steps, the sort included): the cell order of the particles decays
+    # between sorts, which the periods right after the warm-up do not show
+    whole = None
+    if not args.no_whole_run and cfg["sort_every"] > 0:
+        periods = max(1, cfg["sort_every"] // S)
+        barrier()
+        e.synchronize()
+        e.event_record(2)
+        e.run(periods * S)
+        e.event_record(3)
+        wms = max_over_ranks(e.event_elapsed(2, 3), dist)
+        whole = {"periods": periods, "ms_per_step": wms / periods,
+                 "value": aggregate_rate(ws, N, S, periods, wms * 1e-3),
+                 "what": "mean over %d consecutive collision periods (one sort every %d MD steps included)"
+                         % (periods, cfg["sort_every"])}
+
     # e2e: the reference-facing C ABI with host buffers, host<->device copies inside
     e2e = None
     if not args.no_e2e:
@@ -307,7 +331,7 @@ def gpu_arm(args, ws, rk, lr, dist):
                "what": "upload of the full host state, prepare, %d x (collision period + observables), download "
                        "of the full host state" % args.steps}
     return dict(value=value, ms=ms, launches=launches, clocks=clocks, roofline=roofline, e2e=e2e, cfg=cfg,
-                dev_bytes=e.device_bytes())
+                dev_bytes=e.device_bytes(), whole=whole)
 
 
 def main():
@@ -321,6 +345,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-full", action="store_true", help="skip the full-size CPU period")
+    ap.add_argument("--no-whole-run", action="store_true", help="skip the whole-run mean period time")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -343,6 +369,10 @@ def main():
         if rk != 0:
             return 0
         cb = cpu_baseline(args.workload, cycles_max=args.steps + args.warmup, seconds=1e9)
+        # the CPU port runs a bounded sample of the workload: the line names
+        # the box it measured, and the rate is per particle-step
+        conf = dict(conf, workload="%s (bounded CPU sample of: %s)" % (cb["box"], conf["workload"]),
+                    sample_box=cb["box"], measured_on="the sample box; particle-steps/s per particle-step")
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * cb["seconds"] / (args.steps + args.warmup), "higher_is_better": True,
@@ -368,12 +398,19 @@ def main():
         # same trajectory), the faster of the two CPU loop structures
         cc = cpu_baseline(args.workload, seconds=args.cpu_seconds, cell_lists=True)
         cb["cell_list_value"] = cc["value"]
+        if not args.no_cpu_full:
+            # one period of the cell-list port at the workload's full size, to
+            # show that the per-particle-step rate of the sample carries over
+            cf = cpu_baseline(args.workload, cycles_max=1, seconds=1e9, cell_lists=True, full=True)
+            cb["full_config_value"] = cf["value"]
+            cb["full_config_sample"] = cf["sample"] + " (cell-binned pair search)"
     if rk == 0:
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
                 "config": conf, "roofline": r["roofline"], "cpu_baseline": cb, "e2e": r["e2e"],
-                "gpu_launches": r["launches"], "clocks": r["clocks"], "device_bytes": r["dev_bytes"]}
+                "gpu_launches": r["launches"], "clocks": r["clocks"], "device_bytes": r["dev_bytes"],
+                "whole_run": r["whole"]}
         print(json.dumps(line))
     if dist is not None:
         dist.barrier()

@@ -256,10 +256,12 @@ int mpcmd_profile_read(mpcmd_ctx* ctx, double* ms, int64_t* count, int n);
  * library holds until exit; boxes with more shifted cells (lx*ly*lz, or
  * lx*ly*(lz+1) with walls) return MPCMD_ERR_CONFIG.  The first call on a
  * device resolves the array's address (cudaGetSymbolAddress) and must come
- * before any stream capture.  All calls on a device share the array (each
- * clears what it uses): calls that overlap on the GPU race and must be
- * serialised by the caller.  On MPCMD_ERR_CUDA the CUDA error is left for
- * cudaGetLastError. */
+ * before any stream capture; every uncaptured call resolves it again, so after
+ * cudaDeviceReset make the next call outside a capture.  All calls on a device
+ * share the array (each clears what it uses): calls that overlap on the GPU
+ * race and must be serialised by the caller.  A CUDA error already pending on
+ * the calling thread makes the call return MPCMD_ERR_CUDA without launching;
+ * on MPCMD_ERR_CUDA the CUDA error is left for cudaGetLastError. */
 #define MPCMD_STATIC_MAX_CELLS 524288
 int mpcmd_collide_static(const double* x, const double* y, const double* z,
                          double* vx, double* vy, double* vz, int64_t n,

@@ -2829,9 +2829,28 @@ __global__ void k_sub_mean(Dev<T> d, KParams<T> kp) {
   const double mx = d.ctr->sums[8] * inv, my = d.ctr->sums[9] * inv, mz = d.ctr->sums[10] * inv;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
-    d.p.vx[i] = (T)((double)d.p.vx[i] - mx);
-    d.p.vy[i] = (T)((double)d.p.vy[i] - my);
-    d.p.vz[i] = (T)((double)d.p.vz[i] - mz);
+    T* vv[3] = {d.p.vx, d.p.vy, d.p.vz};
+    const double m[3] = {mx, my, mz};
+    for (int c = 0; c < 3; ++c) {
+      const double w = (double)vv[c][i] - m[c];
+      if (sizeof(T) == 8) { vv[c][i] = (T)w; continue; }
+      // FP32: the drawn velocities lie on the float grid and the mean is one
+      // constant, so round-to-nearest would give every velocity of a binade
+      // the same error and leave a net momentum of order N ulp.  Round up or
+      // down at random instead (probability = distance to the other
+      // neighbour over the spacing), from a contract draw of the particle:
+      // unbiased and independent, the residual is a random walk of order
+      // sqrt(N) ulp.
+      float f = (float)w;
+      const double r = w - (double)f;
+      if (r != 0.0) {
+        const float g = nextafterf(f, r > 0.0 ? INFINITY : -INFINITY);
+        double u, unused;
+        contract_pair(kp.seed, TAG_INIT_VEL, (uint32_t)i, (uint32_t)(4 + c), 0, u, unused);
+        if (u * ((double)g - (double)f) * (r > 0.0 ? 1.0 : -1.0) < fabs(r)) f = g;
+      }
+      vv[c][i] = (T)f;
+    }
   }
 }
 

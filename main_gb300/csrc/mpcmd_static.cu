@@ -19,7 +19,11 @@
 //
 // Set-up: the first call on each device (with that device current) resolves
 // the array's device address with cudaGetSymbolAddress, which also loads this
-// module on the device.  Make that first call before any stream capture.
+// module on the device.  Make that first call before any stream capture.  A
+// call on a stream that is not capturing resolves the address again (a host
+// lookup, no allocation), so after cudaDeviceReset the next uncaptured call
+// picks up the reloaded module's array; a captured call uses the address of
+// the last uncaptured one.
 //
 // The arithmetic is the FP64 collision stage of the engine (k_accumulate_main,
 // k_cells and k_rotate_main in mpcmd_kernels.cuh; mpc_rotation_mod.f95:102-228
@@ -128,7 +132,9 @@ extern "C" int mpcmd_collide_static(const double* x, const double* y, const doub
                                     int32_t lz, int32_t geometry, double rot_angle,
                                     int32_t rotation_sense, uint64_t seed, int64_t step,
                                     void* stream) {
-  cudaGetLastError();   // a stale error of this thread is not this call's
+  // An error the calling thread left pending is its own: report it without
+  // launching and leave it in place for the caller's cudaGetLastError.
+  if (cudaPeekAtLastError() != cudaSuccess) return MPCMD_ERR_CUDA;
   if (n < 0 || lx <= 0 || ly <= 0 || lz <= 0 || lx > 1024 || ly > 1024 || lz > 1024) return MPCMD_ERR_CONFIG;
   if (geometry != MPCMD_GEOM_WALLS && geometry != MPCMD_GEOM_PERIODIC) return MPCMD_ERR_CONFIG;
   if (rotation_sense != 1 && rotation_sense != -1) return MPCMD_ERR_CONFIG;
@@ -139,10 +145,13 @@ extern "C" int mpcmd_collide_static(const double* x, const double* y, const doub
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return MPCMD_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return MPCMD_ERR_CONFIG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return MPCMD_ERR_CUDA;
   double* acc = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
       void* p = nullptr;
       if (cudaGetSymbolAddress(&p, g_collide_scratch) != cudaSuccess || !p) return MPCMD_ERR_CUDA;
       g_scratch_ptr[dev] = static_cast<double*>(p);
@@ -167,7 +176,6 @@ extern "C" int mpcmd_collide_static(const double* x, const double* y, const doub
 
   int nsm = 0;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MPCMD_ERR_CUDA;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int64_t want = (n + kThreads - 1) / kThreads;
   const int grid = (int)std::min<int64_t>(want, (int64_t)nsm * 8);
   const int cgrid = (int)std::min<int64_t>((4 * ncs + kThreads - 1) / kThreads, (int64_t)nsm * 8);

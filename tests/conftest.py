@@ -17,6 +17,13 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def reference_root():
+    """Root of a checkout of the reference tree, from MPCMD_REFERENCE_ROOT
+    (None when unset or missing: tests that read the reference decks skip)."""
+    r = os.environ.get("MPCMD_REFERENCE_ROOT")
+    return r if r and os.path.isdir(r) else None
+
+
 def have_gpu():
     try:
         import torch

@@ -1,7 +1,8 @@
 """Regenerate the committed golden fixtures from the reference tree.
 
-Run from the repository root in a container where the reference is mounted:
-    python tests/golden/make_golden.py /root/reference
+Run from the repository root with the reference checkout as the argument
+(or in MPCMD_REFERENCE_ROOT):
+    python tests/golden/make_golden.py <reference root>
 
 hilbert_64x64x32.npz: the cell visiting order of collective_code/hilbert.txt
 (read by sort_hilbert_mod.f95:57-62) as 0-based row-major cell ids (int32,
@@ -26,4 +27,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPCMD_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <reference root> (or set MPCMD_REFERENCE_ROOT)")
+    main(root)

@@ -73,10 +73,11 @@ def test_config_layout_matches_header_and_oracle():
 
 
 def test_reference_decks_parse():
-    ref = "/root/reference"
-    if not os.path.isdir(ref):
+    from conftest import reference_root
+    ref = reference_root()
+    if ref is None:
         import pytest
-        pytest.skip("reference tree not mounted")
+        pytest.skip("MPCMD_REFERENCE_ROOT does not name a reference checkout")
     d = config.read_collective_input(os.path.join(ref, "collective_code", "input.txt"))
     c = config.collective_config(d)
     assert (c["lx"], c["ly"], c["lz"], c["n_dimers"]) == (64, 64, 32, 20)

@@ -143,9 +143,10 @@ def test_anchor_exchange():
 
 
 def test_rotational_decks_parse():
-    ref = "/root/reference/rotational_code"
-    if not os.path.isdir(ref):
-        pytest.skip("reference tree not mounted")
+    from conftest import reference_root
+    if reference_root() is None:
+        pytest.skip("MPCMD_REFERENCE_ROOT does not name a reference checkout")
+    ref = os.path.join(reference_root(), "rotational_code")
     g = config.rotational_config(config.read_rotational_input(os.path.join(ref, "2d_array", "input.txt")))
     assert (g["lx"], g["ly"], g["lz"], g["n_dimers"], g["layout_rows"], g["layout_cols"]) == (64, 64, 32, 36, 6, 6)
     assert g["tether_k"] == 1000.0 and g["tether_z"] == 3.0 and g["mpc_every"] == 20

@@ -56,3 +56,37 @@ def test_static_collision_rejects_boxes_beyond_the_scratch_array():
     assert main_gb300.STATUS[_collide_static(dev, big, 50, 0)] == "invalid configuration"
     torch.cuda.synchronize()
     assert torch.count_nonzero(dev["vx"]).item() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["c0", "c1"])
+def test_static_collision_places_edge_positions_as_the_upload_does(case):
+    """Positions on a wall (z = lz, z just below 0) and outside the periodic
+    box (x = lx + 0.3, y = -0.2) take the same cells in the static entry point
+    as in the context upload, which converts them once."""
+    cfg = CASES[case](64)
+    e = Engine(cfg)
+    e.initial()
+    st = e.download_state()
+    lx, ly, lz = cfg["lx"], cfg["ly"], cfg["lz"]
+    m = 64
+    st["x"][:m] = lx + 0.3
+    st["y"][m:2 * m] = -0.2
+    if cfg["geometry"] == 0:   # walls: the clamp of the z coordinate
+        st["z"][2 * m:3 * m] = float(lz)
+        st["z"][3 * m:4 * m] = -1e-12
+    else:
+        st["z"][2 * m:3 * m] = lz + 0.45
+    e2 = Engine(cfg)
+    e2.upload_state(st)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(st[k])).to("cuda") for k in ("x", "y", "z", "vx", "vy", "vz")}
+    stream = torch.cuda.current_stream().cuda_stream
+    for step in (50, 100):
+        e2.set_step(step)
+        e2.mpc_rotation()
+        ref = e2.download_state()
+        assert _collide_static(dev, cfg, step, stream) == 0
+        torch.cuda.synchronize()
+        for k in ("vx", "vy", "vz"):
+            err = np.abs(dev[k].cpu().numpy() - ref[k]).max()
+            assert err <= VEL_TOL, (case, step, k, err)
