@@ -269,6 +269,99 @@ int mpcmd_collide_static(const double* x, const double* y, const double* z,
                          double rot_angle, int32_t rotation_sense, uint64_t seed,
                          int64_t step, void* stream);
 
+/* Batched ensemble ------------------------------------------------------ */
+/* Many independent single-dimer replicas of the plain periodic run
+ * (collective_code physics with a periodic box: main_pattern.f95:203-225 per
+ * replica, deterministic catalysis forces_mod.f95:79-81, reaction_simple
+ * reaction_mod.f95:8-66, Rodrigues collision mpc_rotation_mod.f95:102-228),
+ * each with its own box, density, sphere sizes, bond, interaction, rate and
+ * seed, advanced together on one GPU.  The reference runs such replicas as
+ * separate jobs of a job array
+ * (rotational_code/linear_periodic_langevin/setup/5_make_subjobs.sh).  Every
+ * replica follows the same step sequence as an mpcmd context of the same
+ * configuration (geometry periodic, one dimer, kinetics simple, exclusion
+ * particle, catalysis deterministic, rotation_sense +1) and the same contract
+ * random streams, so a replica equals its own single-context run up to
+ * rounding.  All replicas share md_dt, mpc_dt, rot_angle, skin, sort_every and
+ * cell_capacity and advance in lockstep; each decides its own list rebuilds on
+ * the device.  One launch per stage covers every replica; mpcmd_ens_run
+ * replays each collision period as one CUDA graph. */
+typedef struct mpcmd_replica {
+  int32_t lx, ly, lz;        /* box edges in cells (4..1024)                        */
+  int32_t reserved;
+  int64_t n_solvent;         /* solvent particles (all species A at mpcmd_ens_initial) */
+  uint64_t seed;             /* contract-stream key of this replica                 */
+  double mass[4];            /* solvent mass per species code                       */
+  double eps_c[4], eps_n[4]; /* LJ strengths of the C and N spheres per species      */
+  double rc, rn, dcn;        /* sphere radii (sigma_C, sigma_N) and bond length      */
+  double mc, mn;             /* sphere masses (0: density-matched, main_pattern.f95:118-119) */
+  double kT;                 /* temperature of the initial velocities               */
+  double k1;                 /* bulk B -> A rate (reaction_mod.f95:41-62)            */
+} mpcmd_replica;
+
+typedef struct mpcmd_ensemble_config {
+  int32_t n_replicas;
+  int32_t precision;         /* MPCMD_PREC_FP32 or MPCMD_PREC_FP64                   */
+  int32_t sort_every;        /* sort_step in MD steps (0 = never)                    */
+  int32_t cell_capacity;     /* per-cell per-species capacity (<= 255)               */
+  int32_t rattle_max_iter;
+  int32_t particle_tile;     /* particles per work tile (0 = from the autotuner cache or 2048) */
+  int32_t block;             /* threads per block of the particle kernels (0 = 256)  */
+  int32_t shell_block;       /* shell entries per tile = threads per block (0 = 256) */
+  double md_dt, mpc_dt, rot_angle, skin;
+} mpcmd_ensemble_config;
+
+typedef struct mpcmd_ens mpcmd_ens;
+
+int mpcmd_ens_create(const mpcmd_ensemble_config* cfg, const mpcmd_replica* replicas, mpcmd_ens** out);
+int mpcmd_ens_destroy(mpcmd_ens* ens);
+int mpcmd_ens_device_bytes(const mpcmd_ens* ens, int64_t* bytes);
+/* initial_mod.f95:6-355 for every replica (the draws of mpcmd_initial). */
+int mpcmd_ens_initial(mpcmd_ens* ens);
+/* State of replica r in the reference layout (as mpcmd_upload_state /
+ * mpcmd_download_state); dpos/dvel/dforce are [2][3]. */
+int mpcmd_ens_upload(mpcmd_ens* ens, int32_t r, const double* x, const double* y, const double* z,
+                     const double* vx, const double* vy, const double* vz, const int32_t* flag,
+                     const double* dpos, const double* dvel, const double* dforce);
+int mpcmd_ens_download(mpcmd_ens* ens, int32_t r, double* x, double* y, double* z, double* vx,
+                       double* vy, double* vz, int32_t* flag, double* dpos, double* dvel,
+                       double* dforce);
+/* main_pattern.f95:168-187 for every replica: sort (at step 0), lists, time_penetrate. */
+int mpcmd_ens_prepare(mpcmd_ens* ens);
+/* nsteps main-loop iterations of every replica; whole collision periods
+ * starting on a period boundary run as graph replays. */
+int mpcmd_ens_run(mpcmd_ens* ens, int64_t nsteps);
+/* Per replica: out[r] as mpcmd_observables. */
+int mpcmd_ens_observables(mpcmd_ens* ens, mpcmd_obs* out);
+/* Propulsion speed (Output_SelkovDimer.f90:168-172: centre-of-mass velocity
+ * along the unit axis C - N) sampled at every collision step since the last
+ * reset: mean[r], and the unit axes of the samples, axes[r][k][3] for
+ * k < min(count, history) (history as given to mpcmd_ens_reset_samples). */
+int mpcmd_ens_reset_samples(mpcmd_ens* ens, int32_t history);
+int mpcmd_ens_samples(mpcmd_ens* ens, double* mean_speed, int64_t* count, float* axes);
+/* Axisymmetric B concentration around each dimer (the steady field the
+ * output_mod.f95:486-603 slabs sample, in the dimer frame): B particles
+ * counted on nz x nr bins of the axial coordinate z in [-zmax, zmax) and the
+ * radius r in [0, rmax) about the dimer midpoint and axis; accumulated at
+ * each call, read as counts[r][nz * nr] (z fastest... see ensemble.py) with
+ * the number of accumulated samples. */
+int mpcmd_ens_field_accumulate(mpcmd_ens* ens, int32_t nz, int32_t nr, double zmax, double rmax);
+int mpcmd_ens_field_read(mpcmd_ens* ens, uint32_t* counts, int64_t* samples);
+/* Work schedule: particle tile, block size of the particle kernels, shell
+ * tile (= block) of the shell kernels.  mpcmd_ens_autotune times candidate
+ * schedules on a snapshot of the state (restored afterwards) and keeps the
+ * fastest; with a cache path it first looks up the shape class of the
+ * ensemble there and records what it measured. */
+int mpcmd_ens_set_schedule(mpcmd_ens* ens, int32_t particle_tile, int32_t block, int32_t shell_block);
+int mpcmd_ens_get_schedule(mpcmd_ens* ens, int32_t* sched /* [3] */);
+int mpcmd_ens_autotune(mpcmd_ens* ens, const char* cache_path, int32_t periods);
+/* Up to n of: kernel launches, graph replays, device status bits, RATTLE
+ * iterations, rebuilds over all replicas, cstep. */
+int mpcmd_ens_counters(mpcmd_ens* ens, int64_t* counters, int32_t n);
+int mpcmd_ens_event_record(mpcmd_ens* ens, int slot);
+int mpcmd_ens_event_elapsed(mpcmd_ens* ens, int a, int b, double* ms);
+int mpcmd_ens_synchronize(mpcmd_ens* ens);
+
 /* Contract random numbers (same streams as the engine), for checkers. */
 double mpcmd_contract_u01(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
                           uint32_t step, int which);

@@ -47,6 +47,23 @@ class MpcmdObs(C.Structure):
     ]
 
 
+class MpcmdReplica(C.Structure):
+    """mpcmd_replica (include/mpcmd.h): one replica of a batched ensemble."""
+    _fields_ = [("lx", C.c_int32), ("ly", C.c_int32), ("lz", C.c_int32), ("reserved", C.c_int32),
+                ("n_solvent", C.c_int64), ("seed", C.c_uint64), ("mass", C.c_double * 4),
+                ("eps_c", C.c_double * 4), ("eps_n", C.c_double * 4), ("rc", C.c_double), ("rn", C.c_double),
+                ("dcn", C.c_double), ("mc", C.c_double), ("mn", C.c_double), ("kT", C.c_double),
+                ("k1", C.c_double)]
+
+
+class MpcmdEnsembleConfig(C.Structure):
+    """mpcmd_ensemble_config (include/mpcmd.h)."""
+    _fields_ = [("n_replicas", C.c_int32), ("precision", C.c_int32), ("sort_every", C.c_int32),
+                ("cell_capacity", C.c_int32), ("rattle_max_iter", C.c_int32), ("particle_tile", C.c_int32),
+                ("block", C.c_int32), ("shell_block", C.c_int32), ("md_dt", C.c_double), ("mpc_dt", C.c_double),
+                ("rot_angle", C.c_double), ("skin", C.c_double)]
+
+
 _lib = None
 
 # Every entry point declared in include/mpcmd.h with its ctypes signature.
@@ -101,6 +118,27 @@ SIGNATURES = {
     "mpcmd_profile": (C.c_int, [_P, C.c_int]),
     "mpcmd_profile_read": (C.c_int, [_P, _dp, _lp, C.c_int]),
     "mpcmd_contract_u01": (C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
+    # batched ensemble
+    "mpcmd_ens_create": (C.c_int, [C.POINTER(MpcmdEnsembleConfig), C.POINTER(MpcmdReplica), C.POINTER(_P)]),
+    "mpcmd_ens_destroy": (C.c_int, [_P]),
+    "mpcmd_ens_device_bytes": (C.c_int, [_P, _lp]),
+    "mpcmd_ens_initial": (C.c_int, [_P]),
+    "mpcmd_ens_upload": (C.c_int, [_P, C.c_int32, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
+    "mpcmd_ens_download": (C.c_int, [_P, C.c_int32, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp]),
+    "mpcmd_ens_prepare": (C.c_int, [_P]),
+    "mpcmd_ens_run": (C.c_int, [_P, C.c_int64]),
+    "mpcmd_ens_observables": (C.c_int, [_P, C.POINTER(MpcmdObs)]),
+    "mpcmd_ens_reset_samples": (C.c_int, [_P, C.c_int32]),
+    "mpcmd_ens_samples": (C.c_int, [_P, _dp, _lp, C.POINTER(C.c_float)]),
+    "mpcmd_ens_field_accumulate": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double, C.c_double]),
+    "mpcmd_ens_field_read": (C.c_int, [_P, C.POINTER(C.c_uint32), _lp]),
+    "mpcmd_ens_set_schedule": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "mpcmd_ens_get_schedule": (C.c_int, [_P, _ip]),
+    "mpcmd_ens_autotune": (C.c_int, [_P, C.c_char_p, C.c_int32]),
+    "mpcmd_ens_counters": (C.c_int, [_P, _lp, C.c_int32]),
+    "mpcmd_ens_event_record": (C.c_int, [_P, C.c_int]),
+    "mpcmd_ens_event_elapsed": (C.c_int, [_P, C.c_int, C.c_int, _dp]),
+    "mpcmd_ens_synchronize": (C.c_int, [_P]),
     # allocation-free collision on caller-owned device arrays (pointers as integers)
     "mpcmd_collide_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32,

@@ -20,8 +20,12 @@ UNITS = [
     ("mpcmd_scan.cu", []),
     ("mpcmd_engine.cu", []),
     ("mpcmd_static.cu", ["--fmad=false"]),
+    ("mpcmd_ensemble_f32.cu", []),
+    ("mpcmd_ensemble_f64.cu", ["--fmad=false"]),
+    ("mpcmd_ensemble.cu", []),
 ]
-HEADERS = ["mpcmd_device.cuh", "mpcmd_engine.cuh", "mpcmd_kernels.cuh"]
+HEADERS = ["mpcmd_device.cuh", "mpcmd_engine.cuh", "mpcmd_kernels.cuh", "mpcmd_ensemble.cuh",
+           "mpcmd_ensemble_impl.cuh", "mpcmd_ensemble_base.h"]
 
 
 def _nvcc():

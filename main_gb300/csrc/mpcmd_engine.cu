@@ -16,16 +16,7 @@
 
 using namespace mpcmd;
 
-namespace {
-
-const double kPi = 3.141592653589793;
-
-// Kernel kinds of the per-launch timing (mpcmd_profile_read order).
-enum {
-  PROF_REBUILD = 0, PROF_FORCE = 1, PROF_DIMER = 2, PROF_CELLS = 3, PROF_ROTATE_MAIN = 4,
-  PROF_SHELL_ADVANCE = 5, PROF_BINS = 6, PROF_FINALIZE = 7, PROF_SORT = 8, PROF_AFFECTED = 9,
-  PROF_KINDS = 10
-};
+namespace mpcmd {
 
 // Hilbert index of a 3-D point (Skilling, "Programming the Hilbert curve",
 // AIP Conf. Proc. 707, 2004): axes -> transpose form, then bit interleave.
@@ -65,6 +56,19 @@ std::vector<int32_t> default_cell_order(int lx, int ly, int lz) {
   for (int64_t k = 0; k < C; ++k) order[(size_t)k] = keys[(size_t)k].second;
   return order;
 }
+
+}  // namespace mpcmd
+
+namespace {
+
+const double kPi = 3.141592653589793;
+
+// Kernel kinds of the per-launch timing (mpcmd_profile_read order).
+enum {
+  PROF_REBUILD = 0, PROF_FORCE = 1, PROF_DIMER = 2, PROF_CELLS = 3, PROF_ROTATE_MAIN = 4,
+  PROF_SHELL_ADVANCE = 5, PROF_BINS = 6, PROF_FINALIZE = 7, PROF_SORT = 8, PROF_AFFECTED = 9,
+  PROF_KINDS = 10
+};
 
 // reactive_grid_mod.f95:8-99 (1-based patch index as in the Fortran).
 std::vector<uint8_t> reactive_table(const mpcmd_config& c) {

@@ -2,6 +2,7 @@
 // orchestration in mpcmd_engine.cu drives.
 #pragma once
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 #include "mpcmd_device.cuh"
 
@@ -207,6 +208,9 @@ struct Launch {
 };
 
 int debug_sync(cudaStream_t st, const char* where, int line);
+// The engine's default cell order of the sort: cells ranked along a Hilbert
+// curve of the box (order[k] = row-major id of the k-th cell).
+std::vector<int32_t> default_cell_order(int lx, int ly, int lz);
 void scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t st);
 int64_t scan_tmp_words(int64_t n);
 extern int64_t g_kernel_launches;
