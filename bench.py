@@ -334,12 +334,179 @@ def gpu_arm(args, ws, rk, lr, dist):
                 dev_bytes=e.device_bytes(), whole=whole)
 
 
+ENSEMBLE_TEXT = ("batched ensemble: %d independent single-dimer periodic replicas, box edge U{16..48}, density "
+                 "U[5,20], sigma_C U[2,5], sigma_N U[1,3], bond sigma_C+sigma_N+U[0.5,1.5], k2 log-U[1e-3,1e-1], "
+                 "own seed each; one launch per stage, one CUDA graph per collision period, autotuned schedule")
+
+
+def ensemble_replicas(n, rank=0):
+    from main_gb300 import ensemble as E
+    return E.sample_replicas(n, seed=1 + rank, base_seed=1000 + 100000 * rank)
+
+
+def cpu_baseline_ensemble(reps, seconds=12.0):
+    """The FP64 oracle (all host cores) running replicas of the ensemble one
+    after the other, as the reference runs its job array, one collision
+    period each, until `seconds` have passed."""
+    from main_gb300 import ensemble as E
+    from oracle.oracle import Oracle
+    import oracle.oracle as O
+    threads = os.cpu_count() or 1
+    done_ps, dt, used = 0, 0.0, 0
+    for rep in reps:
+        cfg = E.config_of_replica(rep, precision=64)
+        o = Oracle(cfg, threads=threads)
+        o.initial()
+        o.prepare()
+        t0 = time.perf_counter()
+        o.run(cfg["mpc_every"])
+        dt += time.perf_counter() - t0
+        done_ps += rep["n_solvent"] * cfg["mpc_every"]
+        used += 1
+        if dt > seconds:
+            break
+    return {"value": done_ps / dt, "unit": UNIT, "cores": O.lib().orc_set_threads(0), "kind": "port",
+            "sample": "the first %d replicas of the ensemble, one after the other, one collision period each "
+                      "after prepare (%d solvent in all)" % (used, sum(r["n_solvent"] for r in reps[:used])),
+            "seconds": dt}
+
+
+def ensemble_arm(args, ws, rk, lr, dist):
+    """Batched ensemble workload: aggregate particle-steps/s over all replicas."""
+    import numpy as np
+    import main_gb300
+    from main_gb300 import ensemble as E
+    main_gb300.set_device(lr)
+    reps = ensemble_replicas(args.replicas, rk)
+    ens = E.Ensemble(reps, precision=32)
+    ens.initial()
+    ens.prepare()
+    cache = os.path.join(ROOT, "main_gb300", "_build", "ensemble_schedules.txt")
+    if args.schedule:
+        ens.set_schedule(*[int(v) for v in args.schedule.split(",")])
+        sched = ens.schedule()
+    else:
+        sched = ens.autotune(cache, periods=2)
+    P = ens.mpc_every
+    N = int(sum(r["n_solvent"] for r in reps))
+    ens.run(args.warmup * P)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    ens.reset_samples(0)
+    barrier()
+    ens.synchronize()
+    with Clocks(lr) as ck:
+        c0 = ens.counters()
+        ens.event_record(0)
+        ens.run(args.steps * P)
+        ens.event_record(1)
+        ms = ens.event_elapsed(0, 1)
+        c1 = ens.counters()
+    barrier()
+    ms = max_over_ranks(ms, dist)
+    value = aggregate_rate(ws, N, P, args.steps, ms * 1e-3)
+    speeds, cnt, _ = ens.samples()
+    obs = ens.observables()
+    shell = sum(o["n_inside"] for o in obs)
+    cells = sum(r["lx"] * r["ly"] * r["lz"] for r in reps)
+    # whole collision period, algorithmic bytes: each particle's 25 B state
+    # read and written once, each shell particle's state every MD step, the
+    # cell table once
+    b = 50.0 * N + 54.0 * shell * P + 8.0 * cells
+    peak, peak_kind = measured_hbm()
+    achieved = b / (ms / args.steps * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "whole collision period (one graph replay)", "achieved": round(achieved, 1),
+                "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": None, "algorithmic_bytes_per_launch": int(b),
+                "what": "B = 50 N + 54 N_shell S + 8 C per period over all replicas, N_shell at the end"}
+    e2e = None
+    if not args.no_e2e:
+        # the public API with host buffers: upload every replica's FP64 state,
+        # prepare, the timed periods with observables, download every replica
+        states = [ens.download(r) for r in range(len(reps))]
+        barrier()
+        t0 = time.perf_counter()
+        for r, stt in enumerate(states):
+            ens.upload(r, stt)
+        ens.prepare()
+        for _ in range(args.steps):
+            ens.run(P)
+            ens.observables()
+        for r in range(len(reps)):
+            ens.download(r)
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+        sb = N * (6 * 8 + 4) + len(reps) * 3 * 3 * 8 * 2
+        e2e = {"value": aggregate_rate(ws, N, P, args.steps, e2e_s), "unit": UNIT,
+               "h2d_bytes_per_step": int(sb / args.steps),
+               "d2h_bytes_per_step": int((sb + args.steps * len(reps) * 200) / args.steps),
+               "what": "upload of every replica's host state, prepare, %d x (collision period + observables), "
+                       "download of every replica" % args.steps}
+    return dict(value=value, ms=ms, launches=c1["launches"] - c0["launches"], clocks=ck.summary(), roofline=roofline,
+                e2e=e2e, reps=reps, N=N, speeds=speeds, samples=cnt, schedule=sched, dev_bytes=ens.device_bytes(),
+                replays=c1["graph_replays"] - c0["graph_replays"], rebuilds=c1["rebuilds"] - c0["rebuilds"])
+
+
+def main_ensemble(args, ws, rk, lr):
+    import numpy as np
+    conf = {"workload": ENSEMBLE_TEXT % args.replicas, "name": "c3", "replicas_per_rank": args.replicas,
+            "md_steps_per_step": 50, "collisions_per_step": 1,
+            "l2": "inputs larger than L2 (resident state >> 129 MB), no flush",
+            "parallelism": "replicas" if ws > 1 else "single"}
+    if args.impl == "reference":
+        if rk != 0:
+            return 0
+        reps = ensemble_replicas(args.replicas, 0)
+        cb = cpu_baseline_ensemble(reps, seconds=max(5.0, args.cpu_seconds))
+        conf["measured_on"] = cb["sample"]
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": conf,
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(lr)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    r = ensemble_arm(args, ws, rk, lr, dist)
+    cb = None
+    if rk == 0 and ws == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline_ensemble(r["reps"], seconds=args.cpu_seconds)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rk == 0:
+        sp = np.asarray(r["speeds"])
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": conf,
+                "roofline": r["roofline"], "cpu_baseline": cb, "e2e": r["e2e"], "gpu_launches": r["launches"],
+                "clocks": r["clocks"], "device_bytes": r["dev_bytes"],
+                "ensemble": {"replicas": len(r["reps"]), "solvent_total": r["N"], "schedule": list(r["schedule"]),
+                             "graph_replays": r["replays"], "rebuilds": r["rebuilds"],
+                             "speed_mean": float(sp.mean()), "speed_min": float(sp.min()),
+                             "speed_max": float(sp.max()), "samples_per_replica": int(np.min(r["samples"])),
+                             "speed_per_replica": [round(float(v), 6) for v in sp]}}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "rot", "rot_line", "rot_owner"])
+    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "c3", "rot", "rot_line", "rot_owner"])
+    ap.add_argument("--replicas", type=int, default=256, help="replicas of the c3 ensemble workload")
+    ap.add_argument("--schedule", default="", help="c3: tile,block,shell_block instead of the autotuner")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--dimers", type=int, default=0, help="override the dimer count (profiling cases)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -351,6 +518,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rk, lr = rank_info()
+
+    if args.workload == "c3":
+        return main_ensemble(args, ws, rk, lr)
 
     from main_gb300 import config
     cfg0 = config.workload(args.workload, scale=args.scale, **({"n_dimers": args.dimers} if args.dimers else {}))

@@ -362,6 +362,48 @@ int mpcmd_ens_event_record(mpcmd_ens* ens, int slot);
 int mpcmd_ens_event_elapsed(mpcmd_ens* ens, int a, int b, double* ms);
 int mpcmd_ens_synchronize(mpcmd_ens* ens);
 
+/* Learned surrogate --------------------------------------------------- */
+/* A multilayer perceptron (n_in inputs -> n_layers hidden layers of width
+ * n_hidden with SiLU -> n_out outputs) trained and evaluated by this
+ * library's own kernels: every contraction runs on the fifth-generation
+ * tensor cores (tcgen05.mma, BF16 operands staged by TMA, FP32 accumulators
+ * in tensor memory); the weights are BF16 in the GEMMs with an FP32 master
+ * copy for Adam.  No counterpart in the reference: it maps replica
+ * parameters to the observables the reference's output routines define
+ * (propulsion speed Output_SelkovDimer.f90:168-172, orientation correlation
+ * 1D_Orientation_Correlation.py:40-53, concentration fields
+ * output_mod.f95:486-603).  x, t, w and y are device pointers (FP32,
+ * row-major); the calls return after their kernels have finished. */
+typedef struct mpcmd_mlp_config {
+  int32_t n_in;              /* 1..64                                               */
+  int32_t n_hidden;          /* multiple of 64, 64..256                             */
+  int32_t n_layers;          /* hidden layers, 1..16                                */
+  int32_t n_out;
+  int32_t batch;             /* training batch, multiple of 128                     */
+  int32_t max_rows;          /* largest mpcmd_mlp_forward batch                     */
+  uint64_t seed;             /* Glorot-uniform initial weights                      */
+  double lr, beta1, beta2, eps;   /* Adam                                          */
+} mpcmd_mlp_config;
+
+typedef struct mpcmd_mlp mpcmd_mlp;
+
+int mpcmd_mlp_create(const mpcmd_mlp_config* cfg, mpcmd_mlp** out);
+int mpcmd_mlp_destroy(mpcmd_mlp* m);
+/* Parameters in FP32, per layer W [n_out_l x n_in_l] row-major then b [n_out_l]. */
+int mpcmd_mlp_param_count(const mpcmd_mlp* m, int64_t* n);
+int mpcmd_mlp_get_params(mpcmd_mlp* m, float* host);
+int mpcmd_mlp_set_params(mpcmd_mlp* m, const float* host);
+/* y [rows, n_out] = network(x [rows, n_in]), rows <= max(batch, max_rows). */
+int mpcmd_mlp_forward(mpcmd_mlp* m, const float* x, int64_t rows, float* y);
+/* Loss sum_j w_j (y_j - t_j)^2 averaged over the batch (x [batch, n_in],
+ * t [batch, n_out], w [n_out]) and its gradients, in the parameter layout
+ * (host array, may be NULL); no update. */
+int mpcmd_mlp_gradients(mpcmd_mlp* m, const float* x, const float* t, const float* w, float* grads,
+                        double* loss);
+/* One Adam step on a batch; loss (may be NULL) before the step. */
+int mpcmd_mlp_train_step(mpcmd_mlp* m, const float* x, const float* t, const float* w, double* loss);
+int mpcmd_mlp_synchronize(mpcmd_mlp* m);
+
 /* Contract random numbers (same streams as the engine), for checkers. */
 double mpcmd_contract_u01(uint64_t seed, uint32_t tag, uint32_t index, uint32_t extra,
                           uint32_t step, int which);

@@ -64,6 +64,13 @@ class MpcmdEnsembleConfig(C.Structure):
                 ("rot_angle", C.c_double), ("skin", C.c_double)]
 
 
+class MpcmdMlpConfig(C.Structure):
+    """mpcmd_mlp_config (include/mpcmd.h)."""
+    _fields_ = [("n_in", C.c_int32), ("n_hidden", C.c_int32), ("n_layers", C.c_int32), ("n_out", C.c_int32),
+                ("batch", C.c_int32), ("max_rows", C.c_int32), ("seed", C.c_uint64), ("lr", C.c_double),
+                ("beta1", C.c_double), ("beta2", C.c_double), ("eps", C.c_double)]
+
+
 _lib = None
 
 # Every entry point declared in include/mpcmd.h with its ctypes signature.
@@ -139,6 +146,16 @@ SIGNATURES = {
     "mpcmd_ens_event_record": (C.c_int, [_P, C.c_int]),
     "mpcmd_ens_event_elapsed": (C.c_int, [_P, C.c_int, C.c_int, _dp]),
     "mpcmd_ens_synchronize": (C.c_int, [_P]),
+    # learned surrogate (device pointers as integers)
+    "mpcmd_mlp_create": (C.c_int, [C.POINTER(MpcmdMlpConfig), C.POINTER(_P)]),
+    "mpcmd_mlp_destroy": (C.c_int, [_P]),
+    "mpcmd_mlp_param_count": (C.c_int, [_P, _lp]),
+    "mpcmd_mlp_get_params": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "mpcmd_mlp_set_params": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "mpcmd_mlp_forward": (C.c_int, [_P, C.c_void_p, C.c_int64, C.c_void_p]),
+    "mpcmd_mlp_gradients": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float), _dp]),
+    "mpcmd_mlp_train_step": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, _dp]),
+    "mpcmd_mlp_synchronize": (C.c_int, [_P]),
     # allocation-free collision on caller-owned device arrays (pointers as integers)
     "mpcmd_collide_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32,

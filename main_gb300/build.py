@@ -23,6 +23,7 @@ UNITS = [
     ("mpcmd_ensemble_f32.cu", []),
     ("mpcmd_ensemble_f64.cu", ["--fmad=false"]),
     ("mpcmd_ensemble.cu", []),
+    ("mpcmd_mlp.cu", []),
 ]
 HEADERS = ["mpcmd_device.cuh", "mpcmd_engine.cuh", "mpcmd_kernels.cuh", "mpcmd_ensemble.cuh",
            "mpcmd_ensemble_impl.cuh", "mpcmd_ensemble_base.h"]

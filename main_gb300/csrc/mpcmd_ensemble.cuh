@@ -130,6 +130,8 @@ struct EDev {
   const int64_t* ct_hi;
   int n_ctiles;
   uint32_t* st_prefix;     // [R + 1] first shell tile of each replica
+  uint32_t* rt_prefix;     // [R + 1] first rebuild tile of each replica (0 tiles when it does not rebuild)
+  int tile;                // particles per tile
   // samples
   float* axes;             // [R * hist * 3]
   int hist;
@@ -194,6 +196,41 @@ __device__ __forceinline__ T block_max(T v, T* sh /* [32] */) {
     for (int i = 0; i < nw; ++i) m = fmax(m, sh[i]);
   __syncthreads();
   return m;
+}
+
+// FP32 build: the eight per-sphere sums of a block, reduced in FP32 (a
+// transposing warp reduction: 9 shuffles for 8 values, lane 4v ends with the
+// warp total of value v), then over the warps in shared memory; thread v < 8
+// returns the block total of value v widened to FP64 (integer ops only), the
+// others 0.  FP64 arithmetic per lane would run at the part's FP64 rate.
+__device__ __forceinline__ double block_sum8_f32(const float (&a)[8], float* sh /* [8 * 32] */) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+  float b[4], c[2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float send = h16 ? a[k] : a[k + 4], keep = h16 ? a[k + 4] : a[k];
+    b[k] = keep + __shfl_xor_sync(full, send, 16);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const float send = h8 ? b[k] : b[k + 2], keep = h8 ? b[k + 2] : b[k];
+    c[k] = keep + __shfl_xor_sync(full, send, 8);
+  }
+  float e = (h4 ? c[1] : c[0]) + __shfl_xor_sync(full, h4 ? c[0] : c[1], 4);
+  e += __shfl_xor_sync(full, e, 2);
+  e += __shfl_xor_sync(full, e, 1);
+  if ((lane & 3) == 0) sh[(lane >> 2) * 32 + w] = e;
+  __syncthreads();
+  double out = 0.;
+  if (threadIdx.x < 8) {
+    float t = 0.f;
+    for (int i = 0; i < nw; ++i) t += sh[threadIdx.x * 32 + i];
+    out = widen_f32(t);
+  }
+  __syncthreads();
+  return out;
 }
 
 template <typename T>
@@ -343,19 +380,58 @@ __global__ void k_ens_download(EDev<T> d, int64_t poff, int64_t n, double* x, do
 // sphere lists hold it: sh_mask) and the E_IN flag, and the largest v^2 of
 // each replica is kept for time_penetrate (:554-564).  mode M_LAZY, M_LISTS
 // or both (a sort runs between the two halves on sort steps).
+// Replica of work tile t of a tile prefix (the largest r with prefix[r] <= t).
+__device__ __forceinline__ int tile_rep(const uint32_t* prefix, int R, unsigned t) {
+  int lo = 0, hi = R - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Plan of a rebuild: the particle tiles of the replicas whose rebuild flag
+// k_ens_dimer set, as a prefix over replicas.  One block.
+template <typename T>
+__global__ void k_ens_plan(EDev<T> d) {
+  __shared__ unsigned part[1024];
+  const int nt = blockDim.x;
+  const int chunk = (d.R + nt - 1) / nt;
+  const int lo = min(d.R, (int)threadIdx.x * chunk), hi = min(d.R, lo + chunk);
+  unsigned local = 0;
+  for (int r = lo; r < hi; ++r)
+    if (d.dyn[r].rebuild) local += (unsigned)((d.rep[r].n + d.tile - 1) / d.tile);
+  part[threadIdx.x] = local;
+  __syncthreads();
+  for (int o = 1; o < nt; o <<= 1) {
+    unsigned v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  unsigned run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (int r = lo; r < hi; ++r) {
+    d.rt_prefix[r] = run;
+    if (d.dyn[r].rebuild) run += (unsigned)((d.rep[r].n + d.tile - 1) / d.tile);
+  }
+  if (threadIdx.x == nt - 1) d.rt_prefix[d.R] = part[nt - 1];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(MAX_BLOCK) k_ens_rebuild(EDev<T> d, int mode) {
   __shared__ T red[32];
-  for (int t = blockIdx.x; t < d.n_ptiles; t += gridDim.x) {
-    const uint32_t r = d.pt_rep[t];
+  const unsigned ntiles = d.rt_prefix[d.R];
+  for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int r = tile_rep(d.rt_prefix, d.R, t);
     Dyn<T>& y = d.dyn[r];
-    if (!y.rebuild) continue;   // uniform over the block
     const Rep<T>& R = d.rep[r];
+    const int64_t tlo = R.poff + (int64_t)(t - d.rt_prefix[r]) * d.tile;
+    const int64_t thi = min(tlo + (int64_t)d.tile, R.poff + R.n);
     const KParams<T>& kp = R.kp;
     const int tc = y.time_count;
     const SphereRel<T> sC = y.srel[0], sN = y.srel[1];
     T vmax = (T)0;
-    for (int64_t i = d.pt_lo[t] + threadIdx.x; i < d.pt_hi[t]; i += blockDim.x) {
+    for (int64_t i = tlo + threadIdx.x; i < thi; i += blockDim.x) {
       uint32_t cell = d.cell[i];
       T ox = d.ox[i], oy = d.oy[i], oz = d.oz[i];
       T vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
@@ -443,16 +519,6 @@ __global__ void k_ens_finalize(EDev<T> d, int shell_block, int advance_step) {
   }
 }
 
-// Replica of shell tile t: the largest r with st_prefix[r] <= t.
-__device__ __forceinline__ int shell_tile_rep(const uint32_t* prefix, int R, unsigned t) {
-  int lo = 0, hi = R - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (prefix[mid] <= t) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // --------------------------------------------------------------- forces ----
 // Over the shell of every replica: LJ 12-6 with each listed sphere within its
 // cutoff and the catalytic A -> B conversion on the C sphere
@@ -464,16 +530,17 @@ __device__ __forceinline__ int shell_tile_rep(const uint32_t* prefix, int R, uns
 template <typename T>
 __global__ void __launch_bounds__(MAX_BLOCK) k_ens_force(EDev<T> d, int mode) {
   __shared__ double red[8 * 32];
+  __shared__ float redf[8 * 32];
   __shared__ T redm[32];
   const unsigned ntiles = d.g->ntiles_s;
   for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int r = shell_tile_rep(d.st_prefix, d.R, t);
+    const int r = tile_rep(d.st_prefix, d.R, t);
     Dyn<T>& y = d.dyn[r];
     const Rep<T>& R = d.rep[r];
     const KParams<T>& kp = R.kp;
     const int64_t j = (int64_t)(t - d.st_prefix[r]) * blockDim.x + threadIdx.x;
     const bool valid = j < (int64_t)y.n_shell;
-    double sums[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+    T sums[8] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0, (T)0, (T)0};
     T msd = (T)0;
     if (valid) {
       const int64_t e = R.soff + j;
@@ -498,8 +565,8 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_ens_force(EDev<T> d, int mode) {
             T fx, fy, fz, u;
             lj(kp, s, E, dR2, dx, dy, dz, fx, fy, fz, u);
             fp[3 * s] = fx; fp[3 * s + 1] = fy; fp[3 * s + 2] = fz;
-            sums[4 * s + 0] -= (double)fx; sums[4 * s + 1] -= (double)fy;
-            sums[4 * s + 2] -= (double)fz; sums[4 * s + 3] += (double)u;
+            sums[4 * s + 0] -= fx; sums[4 * s + 1] -= fy;
+            sums[4 * s + 2] -= fz; sums[4 * s + 3] += u;
           }
         }
       }
@@ -526,10 +593,19 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_ens_force(EDev<T> d, int mode) {
         for (int q = 0; q < 6; ++q) d.sh_fp[6 * e + q] = fp[q];
     }
     if (mode & M_FORCE) {
-      block_sum<8>(sums, red);
-      if (threadIdx.x == 0)
-        for (int q = 0; q < 8; ++q)
-          if (sums[q] != 0.) atomicAdd(&y.facc[q], sums[q]);
+      if (sizeof(T) == 4) {
+        float sf[8];
+        for (int q = 0; q < 8; ++q) sf[q] = (float)sums[q];
+        const double v = block_sum8_f32(sf, redf);
+        if (threadIdx.x < 8 && v != 0.) atomicAdd(&y.facc[threadIdx.x], v);
+      } else {
+        double sd[8];
+        for (int q = 0; q < 8; ++q) sd[q] = (double)sums[q];
+        block_sum<8>(sd, red);
+        if (threadIdx.x == 0)
+          for (int q = 0; q < 8; ++q)
+            if (sd[q] != 0.) atomicAdd(&y.facc[q], sd[q]);
+      }
     }
     if (mode & M_ADVANCE) {
       const T m = block_max(msd, redm);
@@ -555,6 +631,10 @@ __global__ void k_ens_dimer(EDev<T> d, int mode, int rattle_max) {
   const KParams<T>& kp = R.kp;
   const double dt = kp.dtd, Mc = kp.mc, Mn = kp.mn, Dcn = kp.dcn;
   const double hIMc = kp.hIMc, hIMn = kp.hIMn, IIM = kp.IIM;
+  // the FP32 build multiplies by precomputed reciprocals and wraps the
+  // positions once after the iterations (the constraint uses minimum-image
+  // separations); the FP64 build keeps the reference's operation sequence
+  constexpr bool fast = sizeof(T) == 4;
   double X1[3], X2[3], V1[3], V2[3], F1[3], F2[3], Q1[3], Q2[3];
   for (int c = 0; c < 3; ++c) {
     X1[c] = y.dpos[c]; X2[c] = y.dpos[3 + c];
@@ -575,10 +655,18 @@ __global__ void k_ens_dimer(EDev<T> d, int mode, int rattle_max) {
       const double Con2diff = 2.0 * (dV[0] * dd[0] + dV[1] * dd[1] + dV[2] * dd[2]);
       if (fabs(Con2diff) < 1.e-8) break;
       if (acc == rattle_max) { atomicOr(&y.status, E_ERR_RATTLE); break; }
-      const double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
-      for (int c = 0; c < 3; ++c) {
-        V1[c] = V1[c] + 2.0 * O * dd[c] / Mc;
-        V2[c] = V2[c] - 2.0 * O * dd[c] / Mn;
+      if (fast) {
+        const double O2 = -(0.5 * (IIM * Con2diff) * kp.iD2);
+        for (int c = 0; c < 3; ++c) {
+          V1[c] = V1[c] + O2 * dd[c] * kp.iMc;
+          V2[c] = V2[c] - O2 * dd[c] * kp.iMn;
+        }
+      } else {
+        const double O = -(0.25 * (IIM * Con2diff) / (Dcn * Dcn));
+        for (int c = 0; c < 3; ++c) {
+          V1[c] = V1[c] + 2.0 * O * dd[c] / Mc;
+          V2[c] = V2[c] - 2.0 * O * dd[c] / Mn;
+        }
       }
       acc++;
     }
@@ -615,10 +703,11 @@ __global__ void k_ens_dimer(EDev<T> d, int mode, int rattle_max) {
     for (int c = 0; c < 3; ++c) { pr1[c] = X1[c]; pr2[c] = X2[c]; dP[c] = dmi(X1[c] - X2[c], kp.Ld[c]); }
     for (int c = 0; c < 3; ++c) { Q1[c] = V1[c] + hIMc * F1[c]; Q2[c] = V2[c] + hIMn * F2[c]; }
     for (int c = 0; c < 3; ++c) { X1[c] = X1[c] + dt * Q1[c]; X2[c] = X2[c] + dt * Q2[c]; }
-    for (int c = 0; c < 3; ++c) {
-      X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
-      X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
-    }
+    if (!fast)
+      for (int c = 0; c < 3; ++c) {
+        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+      }
     int acc = 0;
     for (;;) {
       double dd[3];
@@ -626,21 +715,45 @@ __global__ void k_ens_dimer(EDev<T> d, int mode, int rattle_max) {
       const double Con1diff = (dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) - Dcn * Dcn;
       if (fabs(Con1diff) < 1.e-6) break;
       if (acc == rattle_max) { atomicOr(&y.status, E_ERR_RATTLE); break; }
-      const double G = -(0.25 * Con1diff * IIM / (dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2]));
-      for (int c = 0; c < 3; ++c) {
-        X1[c] = pr1[c] + Q1[c] * dt + 2.0 * G * dP[c] / Mc;
-        X2[c] = pr2[c] + Q2[c] * dt - 2.0 * G * dP[c] / Mn;
-      }
-      for (int c = 0; c < 3; ++c) {
-        X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
-        X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
-      }
-      for (int c = 0; c < 3; ++c) {
-        Q1[c] = Q1[c] + 2.0 * G * dP[c] / (Mc * dt);
-        Q2[c] = Q2[c] - 2.0 * G * dP[c] / (Mn * dt);
+      const double den = dd[0] * dP[0] + dd[1] * dP[1] + dd[2] * dP[2];
+      if (fast) {
+        // the iteration converges to the tolerance whatever the last bits of
+        // G are: a float reciprocal refined twice replaces the division
+        double rr = (double)__frcp_rn((float)den);
+        rr = rr * (2.0 - den * rr);
+        rr = rr * (2.0 - den * rr);
+        const double G2 = 2.0 * (-(0.25 * Con1diff * IIM) * rr);
+        for (int c = 0; c < 3; ++c) {
+          X1[c] = pr1[c] + Q1[c] * dt + G2 * dP[c] * kp.iMc;
+          X2[c] = pr2[c] + Q2[c] * dt - G2 * dP[c] * kp.iMn;
+          Q1[c] = Q1[c] + G2 * dP[c] * kp.iMcdt;
+          Q2[c] = Q2[c] - G2 * dP[c] * kp.iMndt;
+        }
+      } else {
+        const double G = -(0.25 * Con1diff * IIM / den);
+        for (int c = 0; c < 3; ++c) {
+          X1[c] = pr1[c] + Q1[c] * dt + 2.0 * G * dP[c] / Mc;
+          X2[c] = pr2[c] + Q2[c] * dt - 2.0 * G * dP[c] / Mn;
+        }
+        for (int c = 0; c < 3; ++c) {
+          X1[c] = X1[c] - kp.Ld[c] * floor(X1[c] / kp.Ld[c]);
+          X2[c] = X2[c] - kp.Ld[c] * floor(X2[c] / kp.Ld[c]);
+        }
+        for (int c = 0; c < 3; ++c) {
+          Q1[c] = Q1[c] + 2.0 * G * dP[c] / (Mc * dt);
+          Q2[c] = Q2[c] - 2.0 * G * dP[c] / (Mn * dt);
+        }
       }
       acc++;
     }
+    if (fast)
+      for (int c = 0; c < 3; ++c) {
+        const double L = kp.Ld[c];
+        if (X1[c] >= L) X1[c] -= L; else if (X1[c] < 0.0) X1[c] += L;
+        if (X2[c] >= L) X2[c] -= L; else if (X2[c] < 0.0) X2[c] += L;
+        if (!(X1[c] >= 0.0 && X1[c] < L)) X1[c] = X1[c] - L * floor(X1[c] / L);
+        if (!(X2[c] >= 0.0 && X2[c] < L)) X2[c] = X2[c] - L * floor(X2[c] / L);
+      }
     iters += acc;
     for (int c = 0; c < 3; ++c) {
       y.dpos[c] = X1[c]; y.dpos[3 + c] = X2[c];
@@ -677,26 +790,78 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_ens_collide(EDev<T> d) {
     if (sizeof(T) == 4) { sx = (T)y.shf[0]; sy = (T)y.shf[1]; sz = (T)y.shf[2]; }
     else { sx = (T)y.shift[0]; sy = (T)y.shift[1]; sz = (T)y.shift[2]; }
     const SphereRel<T> sC = y.srel[0], sN = y.srel[1];
-    for (int64_t i = d.pt_lo[t] + threadIdx.x; i < d.pt_hi[t]; i += blockDim.x) {
-      const uint32_t cell = d.cell[i];
-      const T ox = d.ox[i], oy = d.oy[i], oz = d.oz[i];
-      const uint8_t f = d.flag[i];
-      const uint32_t key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
-      d.pkey[i] = key;
-      acc_add<T>(d.acc, R.coff + key, d.vx[i], d.vy[i], d.vz[i]);
-      bool bulk = true;
-      if (f & E_IN) {
-        T dx, dy, dz;
-        if (sep2(kp, cell, ox, oy, oz, sC, dx, dy, dz) <= kp.cut2[0] ||
-            sep2(kp, cell, ox, oy, oz, sN, dx, dy, dz) <= kp.cut2[1])
-          bulk = false;
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    // every lane of a warp takes part in every iteration (the run
+    // aggregation shuffles over the whole warp); lanes past the tile end
+    // carry a key of their own and nothing to add
+    for (int64_t i0 = d.pt_lo[t]; i0 < d.pt_hi[t]; i0 += blockDim.x) {
+      const int64_t i = i0 + threadIdx.x;
+      const bool valid = i < d.pt_hi[t];
+      uint32_t key = 0xFFFFFFFFu - (uint32_t)lane, cid = 0xFFFFFFFFu - (uint32_t)lane;
+      T vx = (T)0, vy = (T)0, vz = (T)0;
+      unsigned cadd = 0u;
+      if (valid) {
+        const uint32_t cell = d.cell[i];
+        const T ox = d.ox[i], oy = d.oy[i], oz = d.oz[i];
+        const uint8_t f = d.flag[i];
+        vx = d.vx[i]; vy = d.vy[i]; vz = d.vz[i];
+        key = shifted_key(kp, cell, ox, oy, oz, sx, sy, sz);
+        d.pkey[i] = key;
+        bool bulk = true;
+        if (f & E_IN) {
+          T dx, dy, dz;
+          if (sep2(kp, cell, ox, oy, oz, sC, dx, dy, dz) <= kp.cut2[0] ||
+              sep2(kp, cell, ox, oy, oz, sN, dx, dy, dz) <= kp.cut2[1])
+            bulk = false;
+        }
+        if (bulk) {
+          const int sp = f & FLAG_SPECIES;
+          cid = unshifted_id(kp.lx, kp.ly, cell);
+          cadd = 1u << (8 * sp);
+          // only the first B of a cell is ever relabelled (reaction_mod.f95:59)
+          if (sp == 1) atomicMin(&d.dfirst[4 * (R.coff + cid) + 1], ((f & E_IN) ? 0x80000000u : 0u) | (uint32_t)i);
+        }
       }
-      if (bulk) {
-        const int sp = f & FLAG_SPECIES;
-        const int64_t c = R.coff + unshifted_id(kp.lx, kp.ly, cell);
-        const unsigned old = atomicAdd(&d.dcnt[c], 1u << (8 * sp));
-        if (((old >> (8 * sp)) & 255u) + 1u > (unsigned)kp.cell_capacity) atomicOr(&y.status, E_ERR_CELL);
-        atomicMin(&d.dfirst[4 * c + sp], ((f & E_IN) ? 0x80000000u : 0u) | (uint32_t)i);
+      // collision sums: runs of equal shifted keys over adjacent lanes (the
+      // particles are in cell order), one atomic per run
+      {
+        const uint32_t prev = __shfl_up_sync(full, key, 1);   // every lane shuffles
+        const unsigned heads = __ballot_sync(full, lane == 0 || prev != key);
+        const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+        T c = valid ? (T)1 : (T)0;
+        for (int o = 1; o < 32; o <<= 1) {
+          const T c2 = __shfl_up_sync(full, c, o), x2 = __shfl_up_sync(full, vx, o);
+          const T y2 = __shfl_up_sync(full, vy, o), z2 = __shfl_up_sync(full, vz, o);
+          if (lane - o >= start) { c += c2; vx += x2; vy += y2; vz += z2; }
+        }
+        const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+        if (tail && valid) {
+          if (sizeof(T) == 4) {
+            atomicAdd(reinterpret_cast<float4*>(d.acc) + (R.coff + key), make_float4((float)c, (float)vx, (float)vy, (float)vz));
+          } else {
+            double* a = reinterpret_cast<double*>(d.acc) + 4 * (R.coff + key);
+            atomicAdd(a + 0, (double)c); atomicAdd(a + 1, (double)vx);
+            atomicAdd(a + 2, (double)vy); atomicAdd(a + 3, (double)vz);
+          }
+        }
+      }
+      // distribute counts: runs of equal unshifted cells, one atomic per run
+      {
+        const uint32_t prev = __shfl_up_sync(full, cid, 1);
+        const unsigned heads = __ballot_sync(full, lane == 0 || prev != cid);
+        const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned a2 = __shfl_up_sync(full, cadd, o);
+          if (lane - o >= start) cadd += a2;
+        }
+        const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+        if (tail && cadd) {
+          const unsigned old = atomicAdd(&d.dcnt[R.coff + cid], cadd);
+          for (int sp = 0; sp < 4; ++sp)
+            if (((old >> (8 * sp)) & 255u) + ((cadd >> (8 * sp)) & 255u) > (unsigned)kp.cell_capacity)
+              atomicOr(&y.status, E_ERR_CELL);
+        }
       }
     }
   }

@@ -189,6 +189,7 @@ struct Ensemble : EnsembleBase {
     Rep<T>* drep = nullptr; Dyn<T>* ddyn = nullptr; Glob* dg = nullptr;
     s |= alloc(drep, R); s |= alloc(ddyn, R); s |= alloc(dg, 1);
     s |= alloc(d.st_prefix, R + 1);
+    s |= alloc(d.rt_prefix, R + 1);
     s |= alloc(d_mass, 4 * (int64_t)R); s |= alloc(d_obs, 8 * (int64_t)R);
     if (s) return MPCMD_ERR_ALLOC;
     d.rep = drep; d.dyn = ddyn; d.g = dg; d.R = R; d.mpc_every = P;
@@ -196,6 +197,7 @@ struct Ensemble : EnsembleBase {
     ECK(cudaMemsetAsync(ddyn, 0, sizeof(Dyn<T>) * R, st));
     ECK(cudaMemsetAsync(dg, 0, sizeof(Glob), st));
     ECK(cudaMemsetAsync(d.st_prefix, 0, sizeof(uint32_t) * (R + 1), st));
+    ECK(cudaMemsetAsync(d.rt_prefix, 0, sizeof(uint32_t) * (R + 1), st));
     ECK(cudaMemsetAsync(d.acc, 0, (sizeof(T) == 4 ? 16 : 32) * (size_t)ctot, st));
     ECK(cudaMemsetAsync(d.dcnt, 0, 4 * (size_t)ctot, st));
     ECK(cudaMemsetAsync(d.dfirst, 0xFF, 16 * (size_t)ctot, st));
@@ -220,6 +222,7 @@ struct Ensemble : EnsembleBase {
     if (pt < 64 || pt > (1 << 20) || b < 32 || b > MAX_BLOCK || b % 32 || sb < 32 || sb > MAX_BLOCK || sb % 32)
       return MPCMD_ERR_CONFIG;
     tile = pt; block = b; sblock = sb;
+    d.tile = pt;
     std::vector<uint32_t> prep, crep;
     std::vector<int64_t> plo, phi, clo, chi;
     for (int r = 0; r < R; ++r) {
@@ -267,6 +270,7 @@ struct Ensemble : EnsembleBase {
   // ---------------------------------------------------------- launches --
   void L_force(int mode) { k_ens_force<T><<<g_shell, sblock, 0, st>>>(d, mode); ++launches; }
   void L_dimer(int mode) { k_ens_dimer<T><<<(R + 127) / 128, 128, 0, st>>>(d, mode, rattle_max); ++launches; }
+  void L_plan() { k_ens_plan<T><<<1, 1024, 0, st>>>(d); ++launches; }
   void L_rebuild(int mode) { k_ens_rebuild<T><<<g_part, block, 0, st>>>(d, mode); ++launches; }
   void L_finalize(int adv) { k_ens_finalize<T><<<1, 1024, 0, st>>>(d, sblock, adv); ++launches; }
   void L_sort() {
@@ -298,6 +302,7 @@ struct Ensemble : EnsembleBase {
     if (need_advance) { L_force(M_ADVANCE); need_advance = false; }
     L_dimer((vel_pending ? M_VEL : 0) | M_POS);
     vel_pending = false;
+    L_plan();
     if (sort_step(s)) {
       L_rebuild(M_LAZY);
       L_sort();
@@ -517,6 +522,7 @@ struct Ensemble : EnsembleBase {
     g.cstep = (unsigned)cstep;
     ECK(cudaMemcpyAsync(d.g, &g, sizeof(g), cudaMemcpyHostToDevice, st));
     if (sort_step(cstep)) L_sort();
+    L_plan();
     L_rebuild(M_LISTS);
     L_finalize(0);
     need_advance = true;
@@ -631,7 +637,8 @@ struct Ensemble : EnsembleBase {
                       {d.vy, sizeof(T) * (size_t)ntot}, {d.vz, sizeof(T) * (size_t)ntot}, {d.flag, (size_t)ntot},
                       {d.sh_idx, 4 * (size_t)stot}, {d.sh_mask, (size_t)stot}, {d.sh_fp, 6 * sizeof(T) * (size_t)stot},
                       {d.sh_msd, sizeof(T) * (size_t)stot}, {d.dyn, sizeof(Dyn<T>) * (size_t)R},
-                      {d.g, sizeof(Glob)}, {d.st_prefix, 4 * (size_t)(R + 1)}};
+                      {d.g, sizeof(Glob)}, {d.st_prefix, 4 * (size_t)(R + 1)},
+                      {d.rt_prefix, 4 * (size_t)(R + 1)}};
       for (auto& rg : snap_regions) {
         void* p = nullptr;
         if (cudaMalloc(&p, rg.second) != cudaSuccess) { release_snapshot(); return MPCMD_ERR_ALLOC; }
