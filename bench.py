@@ -499,12 +499,56 @@ def main_ensemble(args, ws, rk, lr):
     return 0
 
 
+def main_surrogate(args, ws, rk, lr):
+    """Learned surrogate workload: a 4096-point parameter sweep screened by the
+    surrogate with plain-simulation fallback against plain simulation of every
+    point (main_gb300.sweep); the value is the speed-up of the sweep."""
+    if rk != 0:
+        return 0
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the surrogate workload has no reference "
+                          "counterpart; its plain route is timed inside the line of --impl gb300"}))
+        return 0
+    import main_gb300
+    from main_gb300 import sweep
+    main_gb300.set_device(lr)
+    argv = ["--train", str(args.train), "--held-out", str(args.held_out), "--sweep", str(args.sweep),
+            "--periods", str(args.periods), "--epochs", str(args.epochs)]
+    out = sweep.main(argv)
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"])
+        peak_kind = "measured"
+    except Exception:
+        peak, peak_kind = 1900.0, "fallback"
+    inf = out["inference"]
+    sw = out["sweep"]
+    line = {"metric": METRIC, "value": sw["speedup_vs_single_context"], "unit": "x (sweep time plain / surrogate)",
+            "n_gpus": ws, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * sw["screened_s"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (network), f32 (simulation)",
+            "data": "synthetic (seeded replicas simulated by this build)",
+            "config": {"workload": "learned surrogate: MLP 8 -> 4 x 256 SiLU -> 2 + 64 x 32, BF16 weights with FP32 "
+                                   "accumulation, trained on %d batched-ensemble replicas (Adam, lr 1e-3, batch 256); "
+                                   "%d-point sweep screened with plain-simulation fallback; %d collision periods per "
+                                   "run" % (args.train, args.sweep, args.periods), "name": "c4"},
+            "roofline": {"bound": "tensor", "kernel": "k_gemm (forward of %d points)" % inf["points"],
+                         "achieved": round(inf["tflops"], 2), "peak": peak, "peak_source": peak_kind,
+                         "unit": "TFLOP/s", "frac": round(inf["tflops"] / peak, 4), "traffic": None},
+            "surrogate": out}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "c3", "rot", "rot_line", "rot_owner"])
+    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "c3", "c4", "rot", "rot_line", "rot_owner"])
+    ap.add_argument("--train", type=int, default=4096, help="c4: training replicas")
+    ap.add_argument("--held-out", type=int, default=256, help="c4: held-out plain runs")
+    ap.add_argument("--sweep", type=int, default=4096, help="c4: sweep points")
+    ap.add_argument("--periods", type=int, default=500, help="c4: collision periods per run")
+    ap.add_argument("--epochs", type=int, default=60, help="c4: training epochs")
     ap.add_argument("--replicas", type=int, default=256, help="replicas of the c3 ensemble workload")
     ap.add_argument("--schedule", default="", help="c3: tile,block,shell_block instead of the autotuner")
     ap.add_argument("--scale", type=float, default=1.0)
@@ -521,6 +565,8 @@ def main():
 
     if args.workload == "c3":
         return main_ensemble(args, ws, rk, lr)
+    if args.workload == "c4":
+        return main_surrogate(args, ws, rk, lr)
 
     from main_gb300 import config
     cfg0 = config.workload(args.workload, scale=args.scale, **({"n_dimers": args.dimers} if args.dimers else {}))

@@ -152,6 +152,14 @@ int mpcmd_get_anchors(mpcmd_ctx* ctx, double* anchors);
 int mpcmd_set_owner_tags(mpcmd_ctx* ctx, const int32_t* type_b);
 int mpcmd_get_owner_tags(mpcmd_ctx* ctx, int32_t* type_b);
 int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count);
+/* Collision angle, interval and rate constants k[6] (may be NULL: rates
+ * unchanged), as a driver passes rotang to mpc_rotation
+ * (mpc_rotation_mod.f95:6) and MPCt, k1 to reaction_simple
+ * (reaction_mod.f95:8); they apply from the next collision. */
+int mpcmd_set_collision(mpcmd_ctx* ctx, double rot_angle, double mpc_dt, const double* k);
+/* The reactive floor as the driver's react_box array [lx * ly], nonzero =
+ * reactive patch (reactive_grid_mod.f95:8-99 fills it; evolve reads it). */
+int mpcmd_set_reactive_grid(mpcmd_ctx* ctx, const int32_t* table);
 
 /* Reference call surface ----------------------------------------------- */
 int mpcmd_initial(mpcmd_ctx* ctx);        /* initial_mod.f95:6-355                 */

@@ -91,6 +91,8 @@ SIGNATURES = {
     "mpcmd_set_anchors": (C.c_int, [_P, _dp]),
     "mpcmd_get_anchors": (C.c_int, [_P, _dp]),
     "mpcmd_set_step": (C.c_int, [_P, C.c_int64, C.c_int32]),
+    "mpcmd_set_collision": (C.c_int, [_P, C.c_double, C.c_double, _dp]),
+    "mpcmd_set_reactive_grid": (C.c_int, [_P, _ip]),
     "mpcmd_initial": (C.c_int, [_P]),
     "mpcmd_prepare": (C.c_int, [_P]),
     "mpcmd_prepare_restart": (C.c_int, [_P]),

@@ -132,6 +132,8 @@ struct EngineBase {
   virtual int set_owner_tags(const int32_t* t) = 0;
   virtual int get_owner_tags(int32_t* t) = 0;
   virtual int set_step(int64_t cstep, int32_t tc) = 0;
+  virtual int set_collision(double rot_angle, double mpc_dt, const double* k) = 0;
+  virtual int set_reactive_grid(const int32_t* table) = 0;
   virtual int initial() = 0;
   virtual int prepare() = 0;
   virtual int prepare_restart() = 0;
@@ -453,6 +455,30 @@ struct Engine : EngineBase {
     }
     order.assign(o, o + n);
     CK(upload_order());
+    return MPCMD_OK;
+  }
+
+  // Collision angle, interval and rate constants as a driver passes them to
+  // mpc_rotation / reaction_simple (mpc_rotation_mod.f95:6, reaction_mod.f95:8)
+  int set_collision(double rot_angle, double mpc_dt, const double* k) override {
+    if (!(mpc_dt > 0)) return MPCMD_ERR_CONFIG;
+    cfg.rot_angle = rot_angle;
+    cfg.mpc_dt = mpc_dt;
+    kp.cosrot = (T)std::cos(rot_angle);
+    kp.sinrot = (T)std::sin(rot_angle);
+    kp.tau = mpc_dt;
+    kp.tauf = (float)mpc_dt;
+    if (k)
+      for (int q = 0; q < 6; ++q) { cfg.k[q] = k[q]; kp.k[q] = k[q]; kp.kf[q] = (float)k[q]; }
+    return MPCMD_OK;
+  }
+
+  // The reactive floor as the driver's react_box array (reactive_grid_mod.f95:8-99).
+  int set_reactive_grid(const int32_t* table) override {
+    if (!table) return MPCMD_ERR_CONFIG;
+    for (size_t i = 0; i < react.size(); ++i) react[i] = table[i] ? 1 : 0;
+    CK(cudaMemcpyAsync(d.react_box, react.data(), react.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
     return MPCMD_OK;
   }
 
@@ -1522,6 +1548,16 @@ int mpcmd_get_owner_tags(mpcmd_ctx* ctx, int32_t* type_b) {
 int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count) {
   CTX_OK(ctx);
   return ctx->e->set_step(cstep, time_count);
+}
+
+int mpcmd_set_collision(mpcmd_ctx* ctx, double rot_angle, double mpc_dt, const double* k) {
+  CTX_OK(ctx);
+  return ctx->e->set_collision(rot_angle, mpc_dt, k);
+}
+
+int mpcmd_set_reactive_grid(mpcmd_ctx* ctx, const int32_t* table) {
+  CTX_OK(ctx);
+  return ctx->e->set_reactive_grid(table);
 }
 
 int mpcmd_initial(mpcmd_ctx* ctx) { CTX_OK(ctx); return ctx->e->initial(); }
