@@ -39,7 +39,14 @@ typedef enum mpcmd_status {
 enum { MPCMD_GEOM_WALLS = 0, MPCMD_GEOM_PERIODIC = 1 };
 enum { MPCMD_KIN_NONE = 0, MPCMD_KIN_SIMPLE = 1, MPCMD_KIN_SELKOV = 2 };
 enum { MPCMD_EXCL_PARTICLE = 0, MPCMD_EXCL_CELLS = 1 };
-enum { MPCMD_CAT_DETERMINISTIC = 0, MPCMD_CAT_PROBABILISTIC = 1 };
+/* Catalysis on the C sphere: DETERMINISTIC, A -> B at the first force
+ * evaluation inside the C cutoff (forces_mod.f95:79-81); PROBABILISTIC, the
+ * draws of ForcesMD_SelkovDimer.f90:143-198; ON_EXIT, A -> B (probability 1)
+ * when a particle inside a C cutoff at one force evaluation is outside every
+ * C cutoff at the next (the rule of the plain single-dimer workload; not in
+ * the reference's code; owner tags require DETERMINISTIC).  A restart starts
+ * with no particle recorded inside: its force evaluation records them. */
+enum { MPCMD_CAT_DETERMINISTIC = 0, MPCMD_CAT_PROBABILISTIC = 1, MPCMD_CAT_ON_EXIT = 2 };
 enum { MPCMD_PREC_FP32 = 32, MPCMD_PREC_FP64 = 64 };
 /* rotational_code variants: MOTOR is the free dimer of collective_code and
  * selkov_code; ROTOR is the anchored dimer of rotational_code/2d_array and
@@ -60,7 +67,7 @@ typedef struct mpcmd_config {
   int32_t n_dimers;          /* numdims                                             */
   int32_t kinetics;          /* MPCMD_KIN_*: reaction_simple or Selkov RKMPC         */
   int32_t exclusion;         /* MPCMD_EXCL_*: distribute_mod bulk rule or Affected_Cell */
-  int32_t catalysis;         /* MPCMD_CAT_*: forces_mod.f95:79-92 or ForcesMD:302-376 */
+  int32_t catalysis;         /* MPCMD_CAT_*: forces_mod.f95:79-92, ForcesMD:302-376 or on exit */
   int32_t rotation_sense;    /* +1 mpc_rotation_mod Rodrigues, -1 RMPC projection     */
   int32_t mpc_every;         /* MPCtstep                                             */
   int32_t sort_every;        /* sort_step (0 = never)                                */

@@ -38,7 +38,7 @@ FIELDS = [
 GEOM_WALLS, GEOM_PERIODIC = 0, 1
 KIN_NONE, KIN_SIMPLE, KIN_SELKOV = 0, 1, 2
 EXCL_PARTICLE, EXCL_CELLS = 0, 1
-CAT_DETERMINISTIC, CAT_PROBABILISTIC = 0, 1
+CAT_DETERMINISTIC, CAT_PROBABILISTIC, CAT_ON_EXIT = 0, 1, 2
 PREC_FP32, PREC_FP64 = 32, 64
 VARIANT_MOTOR, VARIANT_ROTOR = 0, 1
 LAYOUT_RANDOM, LAYOUT_GRID, LAYOUT_LINE = 0, 1, 2

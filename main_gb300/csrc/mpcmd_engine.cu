@@ -290,6 +290,7 @@ struct Engine : EngineBase {
     if (c.mpc_every <= 0 || c.md_dt <= 0 || c.cell_capacity <= 0 || c.cell_capacity > 255) return MPCMD_ERR_CONFIG;
     if (c.kinetics == MPCMD_KIN_SELKOV && c.geometry != MPCMD_GEOM_PERIODIC) return MPCMD_ERR_CONFIG;
     if (c.variant != MPCMD_VARIANT_MOTOR && c.variant != MPCMD_VARIANT_ROTOR) return MPCMD_ERR_CONFIG;
+    if (c.catalysis < MPCMD_CAT_DETERMINISTIC || c.catalysis > MPCMD_CAT_ON_EXIT) return MPCMD_ERR_CONFIG;
     if (c.variant == MPCMD_VARIANT_ROTOR && !(c.tether_k >= 0.0)) return MPCMD_ERR_CONFIG;
     if (c.owner_tags != 0 &&
         (c.owner_tags != 1 || c.catalysis != MPCMD_CAT_DETERMINISTIC || c.kinetics == MPCMD_KIN_SELKOV ||
@@ -419,6 +420,7 @@ struct Engine : EngineBase {
     // (the variant arrays last: the allocations above keep their placement)
     r |= alloc(d.anchor, 3 * nd1);
     if (c.owner_tags) { r |= alloc(d.owner, n); r |= alloc(d.owner2, n); }
+    if (c.catalysis == MPCMD_CAT_ON_EXIT) { r |= alloc(d.inc, n); r |= alloc(d.inc2, n); }
     if (r) return MPCMD_ERR_ALLOC;
 
     CK(cudaMemsetAsync(d.acc, 0, (sizeof(T) == 4 ? 16 : 32) * (size_t)kp.ncell_shift, st));
@@ -431,6 +433,7 @@ struct Engine : EngineBase {
     CK(cudaMemsetAsync(d.dq, 0, sizeof(double) * 3 * std::max<int64_t>(ns, 1), st));
     CK(cudaMemsetAsync(d.anchor, 0, sizeof(double) * 3 * (size_t)nd1, st));
     if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)n, st));
+    if (d.inc) CK(cudaMemsetAsync(d.inc, 0, (size_t)n, st));
     CK(cudaMemsetAsync(d.p.flag, 0, (size_t)n, st));
     react = reactive_table(c);
     CK(cudaMemcpyAsync(d.react_box, react.data(), react.size(), cudaMemcpyHostToDevice, st));
@@ -542,6 +545,7 @@ struct Engine : EngineBase {
       CK(cudaEventRecord(used[b], st));
     }
     if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)kp.n, st));
+    if (d.inc) CK(cudaMemsetAsync(d.inc, 0, (size_t)kp.n, st));
     CK(cudaMemcpyAsync(d.staging_i, flag, sizeof(int32_t) * kp.n, cudaMemcpyHostToDevice, cst));
     CK(cudaEventRecord(copied[0], cst));
     CK(cudaStreamWaitEvent(st, copied[0], 0));
@@ -1061,6 +1065,7 @@ struct Engine : EngineBase {
     Launch<T>::build_bins(d, kp, 0, st);
     Launch<T>::init_solvent(d, kp, bounds, cfg.kT, cfg.mass, st);
     if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)kp.n, st));
+    if (d.inc) CK(cudaMemsetAsync(d.inc, 0, (size_t)kp.n, st));
     CK(cudaStreamSynchronize(st));
     prepared = false; home_shell = false; advanced = false; n_inside = 0;
     restart_pending = false;

@@ -104,6 +104,8 @@ struct Dev {
   double* fmot;            // [ns*4] motor-motor force and potential (j < k part)
   double* anchor;          // [nd*3] rotor anchors (motorCM)
   uint16_t *owner, *owner2;  // [n] owner tags type_B by main index (null without owner_tags); sort buffer
+  uint8_t *inc, *inc2;     // [n] inside a C cutoff at the last force evaluation, by main index
+                           // (catalysis on exit only, else null); sort buffer
   double* dpot;            // [nd] potential of each dimer at the last force evaluation
   uint32_t* bin_cnt;       // [nbins]
   uint32_t* bin_mask;      // [ceil(nbins / 32)] bit b set: bin b lists a sphere

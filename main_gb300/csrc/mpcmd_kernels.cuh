@@ -715,7 +715,9 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
         if (np > PAIRMAX) { atomicOr(&d.ctr->status, DEV_ERR_PAIR_OVERFLOW); np = PAIRMAX; }
         // a free-flight member must not have entered a cutoff since it was classified
         if ((f & FLAG_PASSIVE) && nonbulk) atomicOr(&d.ctr->status, DEV_ERR_PASSIVE);
-        const bool passive = np > 0 && a.horizon > 0 && !a.mpc &&
+        // (catalysis on exit: a particle inside a C cutoff at the last
+        // force evaluation stays in the shell until one finds it outside)
+        const bool passive = np > 0 && a.horizon > 0 && !a.mpc && !(d.inc && d.inc[i]) &&
                              free_flight_ok(kp, cell, oz, vx, vy, vz, (T)0, min_gap, a.horizon, vs_bound);
         const uint8_t nf = passive ? (uint8_t)(sp | FLAG_PASSIVE) : sp;
         bool placed = false;
@@ -1084,12 +1086,14 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
     const bool keep_pf = !(a.advance && !a.mpc);
     T fpx[PAIRMAX], fpy[PAIRMAX], fpz[PAIRMAX];
     T Fx = (T)0, Fy = (T)0, Fz = (T)0;
+    bool anyC = false, inC = false;   // a C sphere listed / within its cutoff (catalysis on exit)
 #pragma unroll
     for (int q = 0; q < PAIRMAX; ++q) {
       if (!SUMK) fpx[q] = fpy[q] = fpz[q] = (T)0;
       if (!__any_sync(0xffffffffu, q < np)) break;
       int s = (q < np) ? (int)sphl[q] : -1;
       T fx = 0, fy = 0, fz = 0, u = 0;
+      if (s >= 0 && (s & 1) == 0) anyC = true;
       if (s >= 0) {
         const int t = s & 1;
         const SphereRel<T> sr = d.srel[s];
@@ -1107,9 +1111,10 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
             if (t == 0) { fl = (fl & ~FLAG_SPECIES) | 1; own = motor; E = kp.eps_c[1]; }
             else if (spc == 1 && own != motor) E = kp.eps_n[0];
           } else if (t == 0) {
+            inC = true;
             if (kp.catalysis == 0) {
               if (spc == 0) { fl = (fl & ~FLAG_SPECIES) | 1; E = kp.eps_c[1]; }
-            } else if (spc == 0 || spc == 1) {
+            } else if (kp.catalysis == 1 && (spc == 0 || spc == 1)) {
               uint64_t m0, m1;
               contract_bits(kp.seed, TAG_CAT, idx, (uint32_t)s, a.step, m0, m1);
               if (spc == 0 && m0 < kp.thr_ab) fl = (fl & ~FLAG_SPECIES) | 1;
@@ -1131,6 +1136,15 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
         fpx[q] = fx; fpy[q] = fy; fpz[q] = fz;
       }
       warp_sphere_add(d.facc, s, -fx, -fy, -fz, u);
+    }
+    if (act && !OWN && kp.catalysis == 2 && anyC) {
+      // catalysis on exit: an A that was inside a C cutoff at the last force
+      // evaluation and is outside every C cutoff now becomes a B (the pair
+      // forces above use the species before the conversion); a restart's
+      // force evaluation records the state only
+      const bool was = d.inc[idx] != 0;
+      if (was && !inC && !a.forces_only && (fl & FLAG_SPECIES) == 0) fl = (uint8_t)((fl & ~FLAG_SPECIES) | 1);
+      if (was != inC) d.inc[idx] = inC ? 1 : 0;
     }
     if (act) {
       const T h2 = kp.hIM[fl & FLAG_SPECIES];
@@ -1248,7 +1262,7 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
         const uint32_t idx = d.sh.idx[j];
         if (a.watch_build) watch_append(&d.ctr->n_watch, d.watch, idx);
         const T msd_now = d.sh.msd[j];
-        if (free_flight_ok(kp, cell, oz, vx, vy, vz, msd_now, min_gap, a.horizon, vs)) {
+        if (!(d.inc && d.inc[idx]) && free_flight_ok(kp, cell, oz, vx, vy, vz, msd_now, min_gap, a.horizon, vs)) {
           // state of this step into the main home; no force acts before the
           // next rebuild, which streams it with the outside particles
           d.p.cell[idx] = cell;
@@ -2664,6 +2678,7 @@ __global__ void k_sort_gather(Dev<T> d, KParams<T> kp) {
     d.p2.vx[q] = d.p.vx[i]; d.p2.vy[q] = d.p.vy[i]; d.p2.vz[q] = d.p.vz[i];
     d.p2.flag[q] = d.p.flag[i] & FLAG_SPECIES;
     if (d.owner) d.owner2[q] = d.owner[i];
+    if (d.inc) d.inc2[q] = d.inc[i];
   }
 }
 
@@ -2679,6 +2694,7 @@ void Launch<T>::sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
   LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT();
   Particles<T> t = d.p; d.p = d.p2; d.p2 = t;
   uint16_t* o = d.owner; d.owner = d.owner2; d.owner2 = o;
+  uint8_t* c = d.inc; d.inc = d.inc2; d.inc2 = c;
 }
 
 // --------------------------------------------------------------- reductions --

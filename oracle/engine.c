@@ -119,6 +119,8 @@ orc_t* orc_create(const orc_params* p) {
   o->q = calloc(3 * ns, 8);
   o->anchor = calloc(3 * ns, 8);
   o->owner = calloc(n, 4);
+  o->inc = calloc(n, 1);
+  o->cnow = calloc(n, 1);
   o->nbnum = calloc(ns, 8);
   o->nb = calloc(ns * o->maxnb, 8);
   o->fpair = calloc(ns * o->maxnb * 3, 8);
@@ -137,7 +139,7 @@ orc_t* orc_create(const orc_params* p) {
   o->spair = calloc(n * 2 * 3, 8);
   o->spot = calloc(n, 8);
   if (!o->x || !o->y || !o->z || !o->vx || !o->vy || !o->vz || !o->flag || !o->msd ||
-      !o->dpos || !o->dvel || !o->dfrc || !o->q || !o->anchor || !o->owner || !o->nbnum || !o->nb || !o->fpair ||
+      !o->dpos || !o->dvel || !o->dfrc || !o->q || !o->anchor || !o->owner || !o->inc || !o->cnow || !o->nbnum || !o->nb || !o->fpair ||
       !o->pot || !o->in_list || !o->out_list || !o->newcell || !o->cm || !o->axis ||
       !o->ccount || !o->dcount || !o->dfirst || !o->affected || !o->react_box ||
       !o->fsx || !o->fsy || !o->fsz || !o->pfx || !o->pfy || !o->pfz || !o->spair || !o->spot) {
@@ -152,7 +154,7 @@ orc_t* orc_create(const orc_params* p) {
 void orc_destroy(orc_t* o) {
   if (!o) return;
   free(o->x); free(o->y); free(o->z); free(o->vx); free(o->vy); free(o->vz);
-  free(o->flag); free(o->msd); free(o->dpos); free(o->dvel); free(o->dfrc); free(o->q); free(o->anchor); free(o->owner);
+  free(o->flag); free(o->msd); free(o->dpos); free(o->dvel); free(o->dfrc); free(o->q); free(o->anchor); free(o->owner); free(o->inc); free(o->cnow);
   free(o->nbnum); free(o->nb); free(o->fpair); free(o->pot); free(o->in_list);
   free(o->out_list); free(o->newcell); free(o->cm); free(o->axis); free(o->ccount);
   free(o->dcount); free(o->dfirst); free(o->affected); free(o->react_box); free(o->order);
@@ -180,6 +182,7 @@ int orc_set_state(orc_t* o, const double* x, const double* y, const double* z,
   memcpy(o->vx, vx, n * 8); memcpy(o->vy, vy, n * 8); memcpy(o->vz, vz, n * 8);
   memcpy(o->flag, flag, n * 4);
   memset(o->owner, 0, n * 4);
+  memset(o->inc, 0, n);
   if (o->ns > 0) {
     if (dpos) memcpy(o->dpos, dpos, 3 * o->ns * 8);
     if (dvel) memcpy(o->dvel, dvel, 3 * o->ns * 8);
@@ -391,6 +394,9 @@ int orc_sort(orc_t* o) {
   /* linear_periodic_no_ci/sort_hilbert_mod.f95:75,92 carries type_B along */
   for (int64_t j = 0; j < n; ++j) tmpi[j] = o->owner[perm[j]];
   memcpy(o->owner, tmpi, n * 4);
+  /* the inside-a-C-cutoff record of the on-exit catalysis follows the particles */
+  for (int64_t j = 0; j < n; ++j) tmpi[j] = o->inc[perm[j]];
+  for (int64_t j = 0; j < n; ++j) o->inc[j] = (uint8_t)tmpi[j];
   free(cnt); free(start); free(cellid); free(perm); free(tmp); free(tmpi);
   return ORC_OK;
 }
@@ -682,6 +688,7 @@ int orc_initial(orc_t* o) {
   for (int s = 0; s < 3 * o->ns; ++s) { o->dvel[s] = 0.; o->dfrc[s] = 0.; }
   set_midpoint_anchors(o);
   memset(o->owner, 0, (size_t)o->nt * 4);   /* linear_periodic_no_ci/initial_mod.f95:95,146 */
+  memset(o->inc, 0, (size_t)o->nt);
   double* vel[3] = {o->vx, o->vy, o->vz};
   double sum[3] = {0., 0., 0.};
   if (mt) {
@@ -746,10 +753,10 @@ int orc_prepare(orc_t* o) {
 /* restart_mod.f95:415-528: after the lists of a restart, the forces of the
  * restart state (pair forces for the first half kick, catalysis, sphere
  * totals); no kick. */
-static void compute_forces(orc_t* o);
+static void compute_forces(orc_t* o, int restart);
 int orc_restart_forces(orc_t* o) {
   if (!o->prepared) return o->status = ORC_ERR_STATE;
-  compute_forces(o);
+  compute_forces(o, 1);
   return o->status;
 }
 
@@ -781,7 +788,9 @@ static void lj_mot_sol(orc_t* o, int s) {
       double E = eps[f & 3];
       if (tags && !isC && f == 1 && o->owner[i] != motor) E = eps[0];
       if (isC) {
-        if (!prob && tags) {
+        if (o->p.catalysis == ORC_CAT_ON_EXIT) {
+          o->cnow[i] = 1;   /* converted, if at all, after every sphere's pairs (compute_forces) */
+        } else if (!prob && tags) {
           o->flag[i] = 1; o->owner[i] = motor; E = eps[1];
         } else if (!prob) {
           if (f == 0) { o->flag[i] = 1; E = eps[1]; }
@@ -1089,7 +1098,7 @@ static void kick_lists(orc_t* o) {
  * tether of rotational_code/2d_array/evolve_mod.f95:515-531) and :605-636
  * (sphere totals and the potential); restart_mod.f95:415-528 runs the same
  * evaluation at a restart. */
-static void compute_forces(orc_t* o) {
+static void compute_forces(orc_t* o, int restart) {
   const double cut = pow(2.0, 1.0 / 6.0);
   const int rotor = o->p.variant == ORC_VARIANT_ROTOR;
   for (int j = 0; j < 3 * o->ns; ++j) o->dfrc[j] = 0.;
@@ -1136,6 +1145,25 @@ static void compute_forces(orc_t* o) {
     if (o->p.geometry == ORC_GEOM_WALLS) {
       orc_lj_mot_wall(o->L[2], o->dpos[3 * (2 * k) + 2], o->p.ew, o->p.rw + o->p.rc, &fwall[2 * k], &wpot[2 * k]);
       orc_lj_mot_wall(o->L[2], o->dpos[3 * (2 * k + 1) + 2], o->p.ew, o->p.rw + o->p.rn, &fwall[2 * k + 1], &wpot[2 * k + 1]);
+    }
+  }
+  /* catalysis on exit: an A inside a C cutoff at the last evaluation and
+   * outside every C cutoff at this one becomes a B (each C-list member once;
+   * a restart's evaluation records the state only) */
+  if (o->p.catalysis == ORC_CAT_ON_EXIT) {
+    for (int s = 0; s < o->ns; s += 2) {
+      const int64_t base = (int64_t)s * o->maxnb;
+      for (int64_t j = 0; j < o->nbnum[s]; ++j) {
+        const int64_t i = o->nb[base + j];
+        if (o->cnow[i] == 2) continue;
+        if (!restart && o->inc[i] && o->cnow[i] == 0 && (o->flag[i] & 3) == 0) o->flag[i] = 1;
+        o->inc[i] = o->cnow[i] == 1;
+        o->cnow[i] = 2;
+      }
+    }
+    for (int s = 0; s < o->ns; s += 2) {
+      const int64_t base = (int64_t)s * o->maxnb;
+      for (int64_t j = 0; j < o->nbnum[s]; ++j) o->cnow[o->nb[base + j]] = 0;
     }
   }
   /* totals :605-636 */
@@ -1199,7 +1227,7 @@ static void evolve(orc_t* o) {
     o->time_count = 0;
     o->n_rebuilds++;
   }
-  compute_forces(o);
+  compute_forces(o, 0);
   kick_lists(o);
   for (int k = 0; k < o->nd; ++k) {
     if (rotor) rattle_velocities_rotor(o, k);

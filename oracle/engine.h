@@ -16,6 +16,8 @@ struct orc {
   double* q;                  /* RATTLE q vectors [ns*3]                           */
   double* anchor;             /* rotor anchors motorCM [nd*3]                      */
   int32_t* owner;             /* owner tags type_B [nt]                            */
+  uint8_t* inc;               /* inside a C cutoff at the last force evaluation [nt] (catalysis on exit) */
+  uint8_t* cnow;              /* scratch of one force evaluation [nt]              */
   int64_t maxnb;
   int64_t* nbnum;             /* [ns]                                              */
   int64_t* nb;                /* [ns*maxnb]                                        */

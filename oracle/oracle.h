@@ -28,7 +28,10 @@ extern "C" {
 enum { ORC_GEOM_WALLS = 0, ORC_GEOM_PERIODIC = 1 };
 enum { ORC_KIN_NONE = 0, ORC_KIN_SIMPLE = 1, ORC_KIN_SELKOV = 2 };
 enum { ORC_EXCL_PARTICLE = 0, ORC_EXCL_CELLS = 1 };
-enum { ORC_CAT_DETERMINISTIC = 0, ORC_CAT_PROBABILISTIC = 1 };
+/* ON_EXIT: A -> B when a particle inside a C cutoff at one force evaluation
+ * is outside every C cutoff at the next (the plain single-dimer workload's
+ * rule; the reference converts on entry, forces_mod.f95:79-81). */
+enum { ORC_CAT_DETERMINISTIC = 0, ORC_CAT_PROBABILISTIC = 1, ORC_CAT_ON_EXIT = 2 };
 enum { ORC_RNG_CONTRACT = 0, ORC_RNG_MT = 1 };
 /* Pair search of orc_rebuild_lists: every particle against every sphere
  * (neighbour_list_mod.f95, the default), or through cell bins (the same

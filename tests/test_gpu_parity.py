@@ -276,3 +276,21 @@ def test_prepare_restart_matches_oracle(case):
     r.run(63)
     e.run(63)
     assert_close(e.download_state(), r.get_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_catalysis_on_exit(prec):
+    """A -> B on leaving the C interaction shell (MPCMD_CAT_ON_EXIT) against
+    the oracle's restatement of the same rule, over 120 MD steps."""
+    cfg = CASES["c0"](prec, catalysis=config.CAT_ON_EXIT)
+    o, e = pair(cfg)
+    o.prepare()
+    e.prepare()
+    o.run(120)
+    e.run(120)
+    if prec == 64:
+        assert_close(e.download_state(), o.get_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0, dimer=1e-9)
+        assert np.array_equal(o.observables()["species_count"], e.observables()["species_count"])
+    else:
+        assert_close(e.download_state(), o.get_state(), cfg, pos=2e-4, vel=2e-3, flags=0.999, dimer=1e-4)
+    assert o.observables()["species_count"][1] > 0

@@ -296,3 +296,36 @@ def test_cell_list_search_gives_the_same_run(name):
     sa, sb = a.get_state(), b.get_state()
     for k in ("x", "y", "z", "vx", "vy", "vz", "flag", "dpos", "dvel"):
         assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_catalysis_on_exit_converts_exactly_the_leavers():
+    """MPCMD_CAT_ON_EXIT: an A inside the C cutoff at one step's force
+    evaluation and outside it at the next becomes a B, and nothing else
+    changes species (bulk reaction off)."""
+    from main_gb300 import config
+    cfg = config.workload("c0", scale=0.55, precision=64, catalysis=config.CAT_ON_EXIT, k=[0, 0, 0, 0, 0, 0])
+    from oracle.oracle import Oracle
+    o = Oracle(cfg, threads=2)
+    o.initial()
+    o.prepare()
+    L = np.array([cfg["lx"], cfg["ly"], cfg["lz"]], float)
+    cutC = cfg["rc"] * 2.0 ** (1.0 / 6.0)
+
+    def inside(st):
+        d = np.stack([st["x"], st["y"], st["z"]], axis=1) - st["dpos"][0]
+        d -= L * np.round(d / L)
+        return (d * d).sum(axis=1) <= cutC * cutC
+
+    o.step()
+    prev = o.get_state()
+    converted = 0
+    for _ in range(150):
+        o.step()
+        cur = o.get_state()
+        leavers = inside(prev) & ~inside(cur) & (prev["flag"] == 0)
+        expect = prev["flag"].copy()
+        expect[leavers] = 1
+        assert np.array_equal(cur["flag"], expect)
+        converted += int(leavers.sum())
+        prev = cur
+    assert converted > 10, converted
