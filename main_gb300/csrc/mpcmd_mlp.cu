@@ -153,6 +153,7 @@ template <int BN>
 __global__ void __launch_bounds__(THREADS, 1)
     k_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmArgs a) {
   constexpr int B_STAGE = BN * BK * 2;
+  static_assert(BM * (BN + 1) * 4 <= STAGES * (A_STAGE + B_STAGE), "the staged epilogue tile fits the stage ring");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = smem;
@@ -219,39 +220,68 @@ __global__ void __launch_bounds__(THREADS, 1)
   // the tensor memory is read or freed
   __syncthreads();
   const bool done_ok = mbar_wait(done, 0, a.err);
-  const bool have = done_ok && !bail;
+  const bool have = __syncthreads_and(done_ok && !bail) != 0;   // uniform over the CTA
   // epilogue: warp w owns accumulator rows 32w..32w+31
   tmem_fence_after();
   const int m = m0 + warp * 32 + lane;
-  if (have) {
+  const bool staged = a.mode == EP_OUT || a.mode == EP_DW || a.mode == EP_HIDDEN_INFER;
+  if (staged) {
+    // Row-major outputs without a transposed copy go through shared memory:
+    // thread = row in tensor memory, so direct stores would write 32 rows
+    // per instruction; staged, a warp writes one row's contiguous columns.
+    // The tile (128 x (BN + 1) floats, the odd stride keeps both phases free
+    // of bank conflicts) reuses the drained stage ring.
+    float* tile = reinterpret_cast<float*>(smem);
+    constexpr int LD = BN + 1;
+    if (have) {
+      const int r = warp * 32 + lane;
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        const int nb = n0 + c0;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          float o = v[q];
+          if (a.mode != EP_DW) o += a.bias[nb + q];
+          if (a.mode == EP_HIDDEN_INFER) o = o * sigm(o);
+          tile[r * LD + c0 + q] = o;
+        }
+      }
+    }
+    __syncthreads();
+    if (have) {
+      for (int r = warp; r < BM; r += THREADS / 32) {
+        const int mm = m0 + r;
+        if (a.mode != EP_HIDDEN_INFER && mm >= a.m_valid) continue;
+        for (int c = lane; c < BN; c += 32) {
+          const int n = n0 + c;
+          const float o = tile[r * LD + c];
+          if (a.mode == EP_HIDDEN_INFER) a.out_bf16[(size_t)mm * a.ldb + n] = __float2bfloat16_rn(o);
+          else if (a.mode == EP_DW || n < a.n_valid) a.out_f32[(size_t)mm * a.ldo + n] = o;
+        }
+      }
+    }
+  } else if (have) {
     for (int c0 = 0; c0 < BN; c0 += 16) {
       float v[16];
       tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
       const int nb = n0 + c0;
       switch (a.mode) {
-        case EP_HIDDEN:
-        case EP_HIDDEN_INFER: {
+        case EP_HIDDEN: {
           __align__(16) __nv_bfloat16 h[16];
 #pragma unroll
           for (int q = 0; q < 16; ++q) {
             const float z = v[q] + a.bias[nb + q];
-            if (a.mode == EP_HIDDEN) a.z[(size_t)m * a.ldz + nb + q] = z;
+            a.z[(size_t)m * a.ldz + nb + q] = z;
             h[q] = __float2bfloat16_rn(z * sigm(z));
           }
           uint4* dst = reinterpret_cast<uint4*>(a.out_bf16 + (size_t)m * a.ldb + nb);
           dst[0] = reinterpret_cast<const uint4*>(h)[0];
           dst[1] = reinterpret_cast<const uint4*>(h)[1];
-          if (a.mode == EP_HIDDEN)
 #pragma unroll
-            for (int q = 0; q < 16; ++q) a.out_t[(size_t)(nb + q) * a.ldt + m] = h[q];
+          for (int q = 0; q < 16; ++q) a.out_t[(size_t)(nb + q) * a.ldt + m] = h[q];
           break;
         }
-        case EP_OUT:
-          if (m < a.m_valid)
-#pragma unroll
-            for (int q = 0; q < 16; ++q)
-              if (nb + q < a.n_valid) a.out_f32[(size_t)m * a.ldo + nb + q] = v[q] + a.bias[nb + q];
-          break;
         case EP_DX: {
           __align__(16) __nv_bfloat16 g[16];
 #pragma unroll
@@ -267,13 +297,6 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int q = 0; q < 16; ++q) a.out_t[(size_t)(nb + q) * a.ldt + m] = g[q];
           break;
         }
-        case EP_DW:
-          if (m < a.m_valid) {
-            float4* dst = reinterpret_cast<float4*>(a.out_f32 + (size_t)m * a.ldo + nb);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-          }
-          break;
       }
     }
   }
