@@ -164,6 +164,16 @@ int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count);
  * (mpc_rotation_mod.f95:6) and MPCt, k1 to reaction_simple
  * (reaction_mod.f95:8); they apply from the next collision. */
 int mpcmd_set_collision(mpcmd_ctx* ctx, double rot_angle, double mpc_dt, const double* k);
+/* Order-only re-sort every `every` MD steps (a multiple of mpc_every; 0 =
+ * never; default 10 * mpc_every).  At the start of such a collision step the
+ * particles are regrouped in memory by the cell order of sort_hilbert_mod
+ * (the reference's own sort stays at sort_every, sort_hilbert_mod.f95:6-98).
+ * Nothing observable changes: every particle keeps its main index, which
+ * orders the species lists (distribute_mod.f95:95-182), keys the catalysis
+ * draws and indexes every per-particle array this interface reads or writes.
+ * Returns MPCMD_ERR_CONFIG for a negative value or one that is not a multiple
+ * of mpc_every. */
+int mpcmd_set_resort(mpcmd_ctx* ctx, int64_t every);
 /* The reactive floor as the driver's react_box array [lx * ly], nonzero =
  * reactive patch (reactive_grid_mod.f95:8-99 fills it; evolve reads it). */
 int mpcmd_set_reactive_grid(mpcmd_ctx* ctx, const int32_t* table);
@@ -234,7 +244,8 @@ int mpcmd_get_inside(mpcmd_ctx* ctx, int64_t* n_inside, int64_t* idx);
  * iterations, cstep, time_count, pending abort step, last rebuild step,
  * checked-build failure code and value, watch-list entries, and since the last
  * mpcmd_profile(ctx, 1): shell entries over all force launches, particles
- * visited over all rebuild launches, shell entries written by the rebuilds. */
+ * visited over all rebuild launches, shell entries written by the rebuilds;
+ * then the order-only re-sorts run since create. */
 int mpcmd_get_counters(mpcmd_ctx* ctx, int64_t* counters, int32_t n);
 int mpcmd_reactive_grid_table(mpcmd_ctx* ctx, int32_t* table);
 int mpcmd_cell_order(mpcmd_ctx* ctx, int32_t* order);

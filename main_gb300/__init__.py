@@ -92,6 +92,7 @@ SIGNATURES = {
     "mpcmd_get_anchors": (C.c_int, [_P, _dp]),
     "mpcmd_set_step": (C.c_int, [_P, C.c_int64, C.c_int32]),
     "mpcmd_set_collision": (C.c_int, [_P, C.c_double, C.c_double, _dp]),
+    "mpcmd_set_resort": (C.c_int, [_P, C.c_int64]),
     "mpcmd_set_reactive_grid": (C.c_int, [_P, _ip]),
     "mpcmd_initial": (C.c_int, [_P]),
     "mpcmd_prepare": (C.c_int, [_P]),
@@ -300,6 +301,11 @@ class Engine:
     def set_step(self, cstep, time_count=0):
         self._c(lib().mpcmd_set_step(self.h, cstep, time_count), "set_step")
 
+    def set_resort(self, every):
+        """Order-only re-sort every `every` MD steps (a multiple of the
+        collision interval; 0 = never).  Results do not depend on it."""
+        self._c(lib().mpcmd_set_resort(self.h, int(every)), "set_resort")
+
     # -- reference call surface ------------------------------------------
     def initial(self):
         self._c(lib().mpcmd_initial(self.h), "initial")
@@ -430,11 +436,11 @@ class Engine:
         return part[sph == sphere]
 
     def counters(self):
-        c = np.zeros(14, dtype=np.int64)
-        self._c(lib().mpcmd_get_counters(self.h, _ptr(c, C.c_int64), 14), "get_counters")
+        c = np.zeros(15, dtype=np.int64)
+        self._c(lib().mpcmd_get_counters(self.h, _ptr(c, C.c_int64), 15), "get_counters")
         keys = ("n_inside", "status", "time_penetrate", "rattle_iters", "cstep", "time_count", "abort_step",
                 "last_rebuild", "dbg_code", "dbg_val", "n_watch", "work_force_entries", "work_rebuild_particles",
-                "work_rebuild_placed")
+                "work_rebuild_placed", "resorts")
         return dict(zip(keys, (int(v) for v in c)))
 
     def reactive_grid(self):

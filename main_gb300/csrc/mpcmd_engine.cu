@@ -133,6 +133,7 @@ struct EngineBase {
   virtual int get_owner_tags(int32_t* t) = 0;
   virtual int set_step(int64_t cstep, int32_t tc) = 0;
   virtual int set_collision(double rot_angle, double mpc_dt, const double* k) = 0;
+  virtual int set_resort(int64_t every) = 0;
   virtual int set_reactive_grid(const int32_t* table) = 0;
   virtual int initial() = 0;
   virtual int prepare() = 0;
@@ -199,6 +200,11 @@ struct Engine : EngineBase {
   bool restart_pending = false;
   // the watch list of the last collision is valid (no full pass or stage call since)
   bool watch_valid = false;
+  // order-only re-sort every resort_every MD steps (a multiple of the
+  // collision interval; 0 = never): two slot -> index buffers and the
+  // index -> slot table
+  int64_t resort_every = 0, resorts = 0;
+  uint32_t *lid_a = nullptr, *lid_b = nullptr, *lpos_buf = nullptr;
   double w3 = 1.0;
   unsigned int n_inside = 0;
 
@@ -274,7 +280,7 @@ struct Engine : EngineBase {
   int alloc_shell(Shell<T>& s, int64_t cap) {
     int r = 0;
     s.cap = cap;
-    r |= alloc(s.idx, cap); r |= alloc(s.cell, cap);
+    r |= alloc(s.idx, cap); r |= alloc(s.mid, cap); r |= alloc(s.cell, cap);
     r |= alloc(s.ox, cap); r |= alloc(s.oy, cap); r |= alloc(s.oz, cap);
     r |= alloc(s.vx, cap); r |= alloc(s.vy, cap); r |= alloc(s.vz, cap);
     r |= alloc(s.msd, cap); r |= alloc(s.flag, cap); r |= alloc(s.nonbulk, cap); r |= alloc(s.np, cap);
@@ -421,7 +427,12 @@ struct Engine : EngineBase {
     r |= alloc(d.anchor, 3 * nd1);
     if (c.owner_tags) { r |= alloc(d.owner, n); r |= alloc(d.owner2, n); }
     if (c.catalysis == MPCMD_CAT_ON_EXIT) { r |= alloc(d.inc, n); r |= alloc(d.inc2, n); }
+    r |= alloc(lid_a, n); r |= alloc(lid_b, n); r |= alloc(lpos_buf, n);
     if (r) return MPCMD_ERR_ALLOC;
+    d.lid = d.lid2 = d.lpos = nullptr;
+    // a re-sort every ten collision periods (the cell order of a diffusing
+    // solvent decays within a few periods; a re-sort costs about one pass)
+    resort_every = c.mpc_every > 0 ? 10 * (int64_t)c.mpc_every : 0;
 
     CK(cudaMemsetAsync(d.acc, 0, (sizeof(T) == 4 ? 16 : 32) * (size_t)kp.ncell_shift, st));
     CK(cudaMemsetAsync(d.dcnt, 0, 4 * (size_t)kp.ncell, st));
@@ -458,6 +469,33 @@ struct Engine : EngineBase {
     }
     order.assign(o, o + n);
     CK(upload_order());
+    return MPCMD_OK;
+  }
+
+  int set_resort(int64_t every) override {
+    if (every < 0 || (every > 0 && every % cfg.mpc_every != 0)) return MPCMD_ERR_CONFIG;
+    resort_every = every;
+    return MPCMD_OK;
+  }
+
+  // Order-only re-sort at the start of a collision step's rebuild (the lists
+  // that hold slots are rebuilt right after it; the shell learns its
+  // members' new slots).
+  void resort(int tc, int tc_full) {
+    d.lpos = lpos_buf;
+    d.lid2 = d.lid == lid_a ? lid_b : lid_a;
+    Launch<T>::resort(d, kp, tc, tc_full, st);
+    ++resorts;
+  }
+
+  // Main index of every slot (empty while every slot holds the particle of
+  // its own index).
+  int host_lid(std::vector<uint32_t>& v) {
+    v.clear();
+    if (!d.lid) return MPCMD_OK;
+    v.resize((size_t)kp.n);
+    CK(cudaMemcpyAsync(v.data(), d.lid, v.size() * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     return MPCMD_OK;
   }
 
@@ -546,6 +584,7 @@ struct Engine : EngineBase {
     }
     if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)kp.n, st));
     if (d.inc) CK(cudaMemsetAsync(d.inc, 0, (size_t)kp.n, st));
+    d.lid = d.lpos = nullptr;   // the uploaded arrays are in index order
     CK(cudaMemcpyAsync(d.staging_i, flag, sizeof(int32_t) * kp.n, cudaMemcpyHostToDevice, cst));
     CK(cudaEventRecord(copied[0], cst));
     CK(cudaStreamWaitEvent(st, copied[0], 0));
@@ -593,10 +632,14 @@ struct Engine : EngineBase {
 
   int set_owner_tags(const int32_t* t) override {
     if (!d.owner || !t) return MPCMD_ERR_CONFIG;
+    std::vector<uint32_t> lid;
+    int r = host_lid(lid);
+    if (r) return r;
     std::vector<uint16_t> h((size_t)kp.n);
     for (int64_t i = 0; i < kp.n; ++i) {
-      if (t[i] < 0 || t[i] > kp.nd) return MPCMD_ERR_CONFIG;
-      h[(size_t)i] = (uint16_t)t[i];
+      const int32_t v = t[lid.empty() ? i : (int64_t)lid[(size_t)i]];
+      if (v < 0 || v > kp.nd) return MPCMD_ERR_CONFIG;
+      h[(size_t)i] = (uint16_t)v;
     }
     CK(cudaMemcpyAsync(d.owner, h.data(), h.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
@@ -605,10 +648,13 @@ struct Engine : EngineBase {
 
   int get_owner_tags(int32_t* t) override {
     if (!d.owner || !t) return MPCMD_ERR_CONFIG;
+    std::vector<uint32_t> lid;
+    int r = host_lid(lid);
+    if (r) return r;
     std::vector<uint16_t> h((size_t)kp.n);
     CK(cudaMemcpyAsync(h.data(), d.owner, h.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    for (int64_t i = 0; i < kp.n; ++i) t[i] = h[(size_t)i];
+    for (int64_t i = 0; i < kp.n; ++i) t[lid.empty() ? i : (int64_t)lid[(size_t)i]] = h[(size_t)i];
     return MPCMD_OK;
   }
 
@@ -700,9 +746,11 @@ struct Engine : EngineBase {
     a.horizon = (free_flight && !collision_step) ? steps_to_collision(n) : 0;
     a.full = (!free_flight || collision_step) ? 1 : 0;
     bool sort_now = cfg.sort_every > 0 && n % cfg.sort_every == 0;
+    const bool resort_now = !sort_now && mpc && collision_step && resort_every > 0 && n % resort_every == 0;
     if (a.full || sort_now) watch_valid = false;
     a.use_watch = watch_valid ? 1 : 0;
     pb(PROF_BINS); Launch<T>::build_bins(d, kp, a.full ? 0 : a.tc_full, st); pe();
+    if (resort_now) { pb(PROF_SORT); resort(a.tc, a.tc_full); pe(); }
     if (sort_now) {
       StepArgs m = a;
       m.merge_only = 1;
@@ -1064,6 +1112,7 @@ struct Engine : EngineBase {
     CK(cudaMemsetAsync(d.ctr, 0, sizeof(Counters), st));
     Launch<T>::build_bins(d, kp, 0, st);
     Launch<T>::init_solvent(d, kp, bounds, cfg.kT, cfg.mass, st);
+    d.lid = d.lpos = nullptr;
     if (d.owner) CK(cudaMemsetAsync(d.owner, 0, sizeof(uint16_t) * (size_t)kp.n, st));
     if (d.inc) CK(cudaMemsetAsync(d.inc, 0, (size_t)kp.n, st));
     CK(cudaStreamSynchronize(st));
@@ -1207,9 +1256,12 @@ struct Engine : EngineBase {
   }
 
   int get_new_cell(int64_t* out) override {
+    std::vector<uint32_t> lid;
+    int r = host_lid(lid);
+    if (r) return r;
     std::vector<uint32_t> k((size_t)kp.n);
     CK(cudaMemcpy(k.data(), d.skey, k.size() * 4, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < k.size(); ++i) out[i] = k[i];
+    for (size_t i = 0; i < k.size(); ++i) out[lid.empty() ? i : lid[i]] = k[i];
     return MPCMD_OK;
   }
 
@@ -1252,6 +1304,10 @@ struct Engine : EngineBase {
     Counters h;
     int r = read_counters(h);
     if (r) return r;
+    std::vector<uint32_t> lid;
+    r = host_lid(lid);
+    if (r) return r;
+    auto main_index = [&](size_t i) -> int64_t { return lid.empty() ? (int64_t)i : (int64_t)lid[i]; };
     // the shell buffer, then the free-flight members kept in the main home
     std::vector<uint8_t> fl((size_t)kp.n);
     CK(cudaMemcpy(fl.data(), d.p.flag, fl.size(), cudaMemcpyDeviceToHost));
@@ -1262,9 +1318,9 @@ struct Engine : EngineBase {
       std::vector<uint32_t> v(h.n_inside);
       if (h.n_inside) CK(cudaMemcpy(v.data(), d.sh.idx, v.size() * 4, cudaMemcpyDeviceToHost));
       size_t k = 0;
-      for (; k < v.size(); ++k) idx[k] = v[k];
+      for (; k < v.size(); ++k) idx[k] = main_index(v[k]);
       for (size_t i = 0; i < fl.size(); ++i)
-        if (fl[i] & FLAG_PASSIVE) idx[k++] = (int64_t)i;
+        if (fl[i] & FLAG_PASSIVE) idx[k++] = main_index(i);
     }
     return MPCMD_OK;
   }
@@ -1272,6 +1328,9 @@ struct Engine : EngineBase {
   int get_pairs(int64_t* np, int64_t* part, int32_t* sph) override {
     Counters h;
     int r = read_counters(h);
+    if (r) return r;
+    std::vector<uint32_t> lid;
+    r = host_lid(lid);
     if (r) return r;
     size_t m = h.n_inside;
     std::vector<uint32_t> idx(m);
@@ -1285,7 +1344,7 @@ struct Engine : EngineBase {
     int64_t k = 0;
     for (size_t j = 0; j < m; ++j)
       for (int q = 0; q < cnt[j]; ++q) {
-        if (part) part[k] = idx[j];
+        if (part) part[k] = lid.empty() ? (int64_t)idx[j] : (int64_t)lid[idx[j]];
         if (sph) sph[k] = sp[j * PAIRMAX + q];
         ++k;
       }
@@ -1297,11 +1356,11 @@ struct Engine : EngineBase {
     Counters h;
     int r = read_counters(h);
     if (r) return r;
-    int64_t v[14] = {(int64_t)h.n_inside, (int64_t)h.status, (int64_t)h.time_penetrate, (int64_t)h.rattle_iters,
+    int64_t v[15] = {(int64_t)h.n_inside, (int64_t)h.status, (int64_t)h.time_penetrate, (int64_t)h.rattle_iters,
                      (int64_t)cstep, (int64_t)time_count, (int64_t)h.abort_step, (int64_t)last_rebuild,
                      (int64_t)h.dbg_code, (int64_t)h.dbg_val, (int64_t)h.n_watch, (int64_t)h.acc_force,
-                     (int64_t)h.acc_rebuild, (int64_t)h.acc_placed};
-    for (int q = 0; q < n && q < 14; ++q) c[q] = v[q];
+                     (int64_t)h.acc_rebuild, (int64_t)h.acc_placed, resorts};
+    for (int q = 0; q < n && q < 15; ++q) c[q] = v[q];
     return MPCMD_OK;
   }
 
@@ -1558,6 +1617,11 @@ int mpcmd_set_step(mpcmd_ctx* ctx, int64_t cstep, int32_t time_count) {
 int mpcmd_set_collision(mpcmd_ctx* ctx, double rot_angle, double mpc_dt, const double* k) {
   CTX_OK(ctx);
   return ctx->e->set_collision(rot_angle, mpc_dt, k);
+}
+
+int mpcmd_set_resort(mpcmd_ctx* ctx, int64_t every) {
+  CTX_OK(ctx);
+  return ctx->e->set_resort(every);
 }
 
 int mpcmd_set_reactive_grid(mpcmd_ctx* ctx, const int32_t* table) {

@@ -62,7 +62,8 @@ __device__ __forceinline__ bool chk(bool ok, Counters* c, int code, long long v)
 
 template <typename T>
 struct Shell {
-  uint32_t* idx;       // main index
+  uint32_t* idx;       // slot of the member in the main arrays
+  uint32_t* mid;       // its main index (the slot until a re-sort moves particles)
   uint32_t* cell;
   T *ox, *oy, *oz, *vx, *vy, *vz;
   T* msd;              // max_solvent_dist
@@ -106,6 +107,12 @@ struct Dev {
   uint16_t *owner, *owner2;  // [n] owner tags type_B by main index (null without owner_tags); sort buffer
   uint8_t *inc, *inc2;     // [n] inside a C cutoff at the last force evaluation, by main index
                            // (catalysis on exit only, else null); sort buffer
+  // Order-only re-sorts move particles between slots without renumbering
+  // them: lid[slot] is the particle's main index (the index the reference's
+  // arrays hold it at), lpos[index] its slot.  Both null while every slot
+  // holds the particle of the same index (after upload, initial and every
+  // sort of the reference); lid2 is the re-sort's gather target.
+  uint32_t *lid, *lid2, *lpos;
   double* dpot;            // [nd] potential of each dimer at the last force evaluation
   uint32_t* bin_cnt;       // [nbins]
   uint32_t* bin_mask;      // [ceil(nbins / 32)] bit b set: bin b lists a sphere
@@ -200,6 +207,10 @@ struct Launch {
   static void flush(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void regather(const Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
   static void sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st);
+  // order-only re-sort: particles grouped by the sort rank of their stored
+  // cell (any order inside a cell), main indices kept in lid / lpos; the
+  // caller provides lid2 and lpos and swaps nothing
+  static void resort(Dev<T>& d, const KParams<T>& kp, int tc, int tc_full, cudaStream_t st);
   static void observables(const Dev<T>& d, const KParams<T>& kp, const double* mass, int grid, cudaStream_t st);
   static void concentration(const Dev<T>& d, const KParams<T>& kp, int tc, int tc_defer, const ConcArgs& c,
                             cudaStream_t st);

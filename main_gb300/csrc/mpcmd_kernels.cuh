@@ -44,6 +44,13 @@ __device__ __forceinline__ void accum_dist(const Dev<T>& d, const KParams<T>& kp
   atomicMin(&d.dfirst[4 * (size_t)cid + sp], key);
 }
 
+// Main index of the particle in slot i (slot = index until an order-only
+// re-sort moves particles).
+template <typename T>
+__device__ __forceinline__ uint32_t lid_of(const Dev<T>& d, uint32_t i) {
+  return d.lid ? d.lid[i] : i;
+}
+
 // Ordering key of a species-list member: group (0 outside, 1 inside when the
 // lists put the inside particles last) above the main index (< 2^31).  The
 // smallest key of a cell is its first member; 0xFFFFFFFF is "none".
@@ -249,8 +256,8 @@ void Launch<T>::upload_flag(const Dev<T>& d, const KParams<T>& kp, const int32_t
 // or with `current` every particle at the current step (outside particles
 // written at the last rebuild streamed by tc, deferred ones by tc_defer + tc).
 template <typename T>
-__global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_box, double* out, int comp, int tc,
-                           int tc_defer, int current) {
+__global__ void k_download(Particles<T> p, const uint32_t* lid, KParams<T> kp, const uint8_t* react_box, double* out,
+                           int comp, int tc, int tc_defer, int current) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
     uint32_t c = p.cell[i];
@@ -270,14 +277,14 @@ __global__ void k_download(Particles<T> p, KParams<T> kp, const uint8_t* react_b
     else if (comp == 1) v = (double)cell_y(c) + (double)oy;
     else if (comp == 2) v = (double)cell_z(c) + (double)oz;
     else v = (double)(comp == 3 ? vx : comp == 4 ? vy : vz);
-    out[i] = v;
+    out[lid ? lid[i] : i] = v;
   }
 }
 
 template <typename T>
 void Launch<T>::download_convert(const Dev<T>& d, const KParams<T>& kp, double* out, int comp, int tc,
                                  int tc_defer, int current, cudaStream_t st) {
-  k_download<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, comp, tc, tc_defer, current);
+  k_download<T><<<1024, TPB, 0, st>>>(d.p, d.lid, kp, d.react_box, out, comp, tc, tc_defer, current);
   LAUNCH_COUNT();
 }
 
@@ -350,8 +357,8 @@ void Launch<T>::concentration(const Dev<T>& d, const KParams<T>& kp, int tc, int
 // k_download, so a reactive-floor hit in that time (reactive_grid_mod.f95:
 // 103-151) changes the species it reports.
 template <typename T>
-__global__ void k_download_flag(Particles<T> p, KParams<T> kp, const uint8_t* react_box, int32_t* out, int tc,
-                                int tc_defer, int current) {
+__global__ void k_download_flag(Particles<T> p, const uint32_t* lid, KParams<T> kp, const uint8_t* react_box,
+                                int32_t* out, int tc, int tc_defer, int current) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < kp.n; i += stride) {
     uint8_t f = p.flag[i];
@@ -366,14 +373,14 @@ __global__ void k_download_flag(Particles<T> p, KParams<T> kp, const uint8_t* re
         stream_one(kp, react_box, c, ox, oy, oz, vx, vy, vz, f, true, lag);
       }
     }
-    out[i] = f & FLAG_SPECIES;
+    out[lid ? lid[i] : i] = f & FLAG_SPECIES;
   }
 }
 
 template <typename T>
 void Launch<T>::download_flag(const Dev<T>& d, const KParams<T>& kp, int32_t* out, int tc, int tc_defer,
                               int current, cudaStream_t st) {
-  k_download_flag<T><<<1024, TPB, 0, st>>>(d.p, kp, d.react_box, out, tc, tc_defer, current);
+  k_download_flag<T><<<1024, TPB, 0, st>>>(d.p, d.lid, kp, d.react_box, out, tc, tc_defer, current);
   LAUNCH_COUNT();
 }
 
@@ -596,13 +603,17 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
   auto pidx = [&](int64_t k) -> int64_t { return listed ? (int64_t)d.watch[k] : k; };
   const int64_t first = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31) + lane;
   uint8_t pf_f = 0;
-  uint32_t pf_cell = 0;
+  uint32_t pf_cell = 0, pf_lid = 0;   // (the main index only after a re-sort)
   T pf_ox = 0, pf_oy = 0, pf_oz = 0, pf_vx = 0, pf_vy = 0, pf_vz = 0;
+  // (the species lists of a collision step need it for every particle; a
+  // placed shell member of another rebuild loads its own)
+  const bool want_lid = d.lid && a.mpc && kp.kinetics != 0 && !a.merge_only;
   if (first < nloop) {
     const int64_t q = pidx(first);
     pf_f = d.p.flag[q]; pf_cell = d.p.cell[q];
     pf_ox = d.p.ox[q]; pf_oy = d.p.oy[q]; pf_oz = d.p.oz[q];
     pf_vx = d.p.vx[q]; pf_vy = d.p.vy[q]; pf_vz = d.p.vz[q];
+    if (want_lid) pf_lid = d.lid[q];
   }
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < nloop; base += stride) {
     const int64_t k = base + lane;
@@ -612,6 +623,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
     uint8_t sp = 0;
     uint8_t f = pf_f;
     uint32_t cell = pf_cell;
+    const uint32_t my_lid = want_lid ? pf_lid : (uint32_t)i;
     T ox = pf_ox, oy = pf_oy, oz = pf_oz;
     T vx = pf_vx, vy = pf_vy, vz = pf_vz;
     const int64_t knext = k + stride;
@@ -620,6 +632,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
       pf_f = d.p.flag[q]; pf_cell = d.p.cell[q];
       pf_ox = d.p.ox[q]; pf_oy = d.p.oy[q]; pf_oz = d.p.oz[q];
       pf_vx = d.p.vx[q]; pf_vy = d.p.vy[q]; pf_vz = d.p.vz[q];
+      if (want_lid) pf_lid = d.lid[q];
     }
     if (k < nloop) {
       const uint32_t cell0 = cell;
@@ -731,6 +744,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
             atomicOr(&d.ctr->status, DEV_ERR_SHELL_OVERFLOW);
           } else {
             d.sh2.idx[j] = (uint32_t)i;
+            d.sh2.mid[j] = want_lid ? my_lid : lid_of(d, (uint32_t)i);
             d.sh2.cell[j] = cell;
             d.sh2.ox[j] = ox; d.sh2.oy[j] = oy; d.sh2.oz[j] = oz;
             d.sh2.vx[j] = vx; d.sh2.vy[j] = vy; d.sh2.vz[j] = vz;
@@ -778,10 +792,11 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild(Dev<T> d, KParams<T> kp, Ste
       const unsigned dmask = __ballot_sync(0xffffffffu, dist);
       unsigned peers = 0u;
       if (dist) peers = __match_any_sync(dmask, (cid << 2) | (uint32_t)sp);
-      // a listed pass holds its particles in list order, not index order:
-      // the group's smallest index is reduced over its lanes
-      uint32_t first_i = (uint32_t)i;
-      if (dist && listed) first_i = __reduce_min_sync(peers, (uint32_t)i);
+      // a listed pass holds its particles in list order, and re-sorted slots
+      // are not in index order: the group's smallest index is reduced over
+      // its lanes
+      uint32_t first_i = dist ? my_lid : 0u;
+      if (dist && (listed || d.lid)) first_i = __reduce_min_sync(peers, first_i);
       if (dist && lane == __ffs(peers) - 1) {
         // the count returned by this atomic is checked one iteration later,
         // so that the warp does not wait for it
@@ -848,18 +863,20 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
     return st + 1 < FAR_STEPS ? j + TPB : j - (uint32_t)(FAR_STEPS - 1) * TPB + tile_stride;
   };
   uint8_t pf_f = FLAG_HOME_SHELL;
-  uint32_t pf_cell = 0;
+  uint32_t pf_cell = 0, pf_lid = 0;   // (the main index only after a re-sort)
   T pf_ox = 0, pf_oy = 0, pf_oz = 0, pf_vx = 0, pf_vy = 0, pf_vz = 0;
   if (i < n32) {
     pf_f = d.p.flag[i]; pf_cell = d.p.cell[i];
     pf_ox = d.p.ox[i]; pf_oy = d.p.oy[i]; pf_oz = d.p.oz[i];
     pf_vx = d.p.vx[i]; pf_vy = d.p.vy[i]; pf_vz = d.p.vz[i];
+    if (distrib && d.lid) pf_lid = d.lid[i];
   }
   // the loop runs while the warp's step base is inside the array (warp-uniform)
   for (; i - lane < n32; i = advance(i, step), step = step + 1 < FAR_STEPS ? step + 1 : 0) {
     const bool in = i < n32;
     const uint8_t f = pf_f;
     uint32_t cell = pf_cell;
+    const uint32_t my_lid = pf_lid;
     T ox = pf_ox, oy = pf_oy, oz = pf_oz;
     T vx = pf_vx, vy = pf_vy, vz = pf_vz;
     const uint32_t inext = advance(i, step);
@@ -867,6 +884,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
       pf_f = d.p.flag[inext]; pf_cell = d.p.cell[inext];
       pf_ox = d.p.ox[inext]; pf_oy = d.p.oy[inext]; pf_oz = d.p.oz[inext];
       pf_vx = d.p.vx[inext]; pf_vy = d.p.vy[inext]; pf_vz = d.p.vz[inext];
+      if (distrib && d.lid) pf_lid = d.lid[inext];
     }
     bool far = in && !(f & FLAG_HOME_SHELL);
     bool near = in && !far;
@@ -916,13 +934,17 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
       const unsigned dmask = __ballot_sync(0xffffffffu, dist);
       unsigned peers = 0u;
       if (dist) peers = __match_any_sync(dmask, (cid << 2) | (uint32_t)sp);
+      // the group's lowest lane holds its smallest index unless re-sorted
+      // slots put the indices out of order
+      uint32_t first_i = (uint32_t)i;
+      if (dist && d.lid) first_i = __reduce_min_sync(peers, my_lid);
       if (dist && lane == __ffs(peers) - 1) {
         if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
           atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
         pend_cnt = __popc(peers);
         pend_shift = 8 * sp;
         pend_old = atomicAdd(&d.dcnt[cid], pend_cnt << pend_shift);
-        atomicMin(&d.dfirst[4 * (size_t)cid + sp], dist_key(0, (uint32_t)i));
+        atomicMin(&d.dfirst[4 * (size_t)cid + sp], dist_key(0, first_i));
       }
     }
   }
@@ -1068,7 +1090,10 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
       vx = d.sh.vx[j]; vy = d.sh.vy[j]; vz = d.sh.vz[j];
       fl = d.sh.flag[j];
       np = d.sh.np[j];
-      idx = d.sh.idx[j];
+      // the main index keys the catalysis draws and orders the species lists;
+      // without owner tags or the on-exit record nothing here needs the slot,
+      // so after a re-sort the entry's main index replaces it
+      idx = (d.lid && !OWN && !d.inc) ? d.sh.mid[j] : d.sh.idx[j];
       const uint4 packed = *reinterpret_cast<const uint4*>(d.sh.sph + (size_t)j * PAIRMAX);
       sphl[0] = (uint16_t)(packed.x & 0xFFFFu); sphl[1] = (uint16_t)(packed.x >> 16);
       sphl[2] = (uint16_t)(packed.y & 0xFFFFu); sphl[3] = (uint16_t)(packed.y >> 16);
@@ -1116,7 +1141,7 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
               if (spc == 0) { fl = (fl & ~FLAG_SPECIES) | 1; E = kp.eps_c[1]; }
             } else if (kp.catalysis == 1 && (spc == 0 || spc == 1)) {
               uint64_t m0, m1;
-              contract_bits(kp.seed, TAG_CAT, idx, (uint32_t)s, a.step, m0, m1);
+              contract_bits(kp.seed, TAG_CAT, (OWN || d.inc) ? lid_of(d, idx) : idx, (uint32_t)s, a.step, m0, m1);
               if (spc == 0 && m0 < kp.thr_ab) fl = (fl & ~FLAG_SPECIES) | 1;
               if (spc == 1 && m0 < kp.thr_ba) fl = (fl & ~FLAG_SPECIES) | 0;
             }
@@ -1165,7 +1190,7 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
           bool bulk = kp.exclusion == 1 || !d.sh.nonbulk[j];
           if (bulk)
             accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), fl & FLAG_SPECIES,
-                       dist_key(kp.exclusion == 0 ? 1 : 0, idx));
+                       dist_key(kp.exclusion == 0 ? 1 : 0, (OWN || d.inc) ? lid_of(d, idx) : idx));
         }
       }
       if (a.advance && !a.mpc) {
@@ -1281,6 +1306,7 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
         const unsigned int k = bslot + g.thread_rank();
         if ((int64_t)k >= d.sh2.cap) { atomicOr(&d.ctr->status, DEV_ERR_SHELL_OVERFLOW); continue; }
         d.sh2.idx[k] = idx;
+        d.sh2.mid[k] = d.sh.mid[j];
         d.sh2.cell[k] = cell;
         d.sh2.ox[k] = ox; d.sh2.oy[k] = oy; d.sh2.oz[k] = oz;
         d.sh2.vx[k] = vx; d.sh2.vy[k] = vy; d.sh2.vz[k] = vz;
@@ -1416,6 +1442,7 @@ __global__ void k_shell_scatter(Dev<T> d, KParams<T> kp) {
     if (!chk((int64_t)k < d.sh.cap, d.ctr, 125, k)) continue;
     const uint32_t idx = d.sh2.idx[j];
     d.sh.idx[k] = idx;
+    d.sh.mid[k] = d.sh2.mid[j];
     d.sh.cell[k] = d.sh2.cell[j];
     d.sh.ox[k] = d.sh2.ox[j]; d.sh.oy[k] = d.sh2.oy[j]; d.sh.oz[k] = d.sh2.oz[j];
     d.sh.vx[k] = d.sh2.vx[j]; d.sh.vy[k] = d.sh2.vy[j]; d.sh.vz[k] = d.sh2.vz[j];
@@ -2195,7 +2222,7 @@ __global__ void __launch_bounds__(TPB) k_accumulate_main(Dev<T> d, KParams<T> kp
       }
       if (bulk)
         accum_dist(d, kp, unshifted_id(kp.lx, kp.ly, cell), f & FLAG_SPECIES,
-                   dist_key(kp.exclusion == 0 && inl ? 1 : 0, (uint32_t)i));
+                   dist_key(kp.exclusion == 0 && inl ? 1 : 0, lid_of(d, (uint32_t)i)));
     }
   }
 }
@@ -2212,7 +2239,7 @@ void Launch<T>::accumulate_main(const Dev<T>& d, const KParams<T>& kp, const Ste
 // the main arrays.
 template <typename T>
 __device__ __forceinline__ void relabel_key(const Dev<T>& d, uint32_t key, int code) {
-  const uint32_t idx = key & 0x7FFFFFFFu;
+  const uint32_t idx = d.lpos ? d.lpos[key & 0x7FFFFFFFu] : key & 0x7FFFFFFFu;
   const uint8_t f = d.p.flag[idx];
   // B -> A clears the owner tag (linear_periodic_no_ci/reaction_simple_mod.f95:55)
   if (d.owner && code == 0) d.owner[idx] = 0;
@@ -2657,11 +2684,12 @@ __global__ void k_sort_segments(Dev<T> d, KParams<T> kp) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < kp.ncell; r += stride) {
     uint32_t b = d.sstart[r], n = d.scnt[r];
     if (!chk((int64_t)b + n <= kp.n, d.ctr, 106, (long long)b + n)) continue;
+    // by main index: the slots of re-sorted particles are not in index order
     uint32_t* s = d.sidx + b;
     for (uint32_t i = 1; i < n; ++i) {
-      uint32_t v = s[i];
+      const uint32_t v = s[i], kv = lid_of(d, v);
       int j = (int)i - 1;
-      while (j >= 0 && s[j] > v) { s[j + 1] = s[j]; --j; }
+      while (j >= 0 && lid_of(d, s[j]) > kv) { s[j + 1] = s[j]; --j; }
       s[j + 1] = v;
     }
   }
@@ -2682,6 +2710,241 @@ __global__ void k_sort_gather(Dev<T> d, KParams<T> kp) {
   }
 }
 
+// Order-only re-sort.  The reference keeps its arrays in index order between
+// sorts; here particles may move to other slots in between, keeping their
+// main index (lid / lpos), so that the slots follow the cell order while the
+// particles diffuse.  It runs at the start of a collision step's rebuild and
+// groups every particle by the sort rank of the cell it is in at that step
+// (a shell-resident particle: its shell cell; a lazily streamed one: its
+// stored state streamed over its lag, the same flight the collision pass
+// then makes), in any order inside a cell.  The records move as stored
+// (lagging states and flags included), and a shell slot learns its
+// member's new slot.
+//
+// Two levels, so that no pass needs an atomic per particle: bins of 2^bits
+// consecutive ranks (up to a thousand particles on average; a warp of the
+// nearly sorted slots meets one or two bins, one aggregated atomic each),
+// then a counting sort of each bin in shared memory.  Scratch: the rank of
+// every slot in skey, the bin lists (slot, rank) in sidx / watch; none of
+// them is live at the start of a collision step's rebuild.
+constexpr int RESORT_MAX_BITS = 8;   // at most 256 ranks per bin (one per thread of the fine pass)
+constexpr int RESORT_UNROLL = 4;     // 32-particle steps per warp with their loads issued first
+constexpr int RESORT_CAP = 2048;     // members of a bin sorted in shared memory (larger: bin order kept)
+
+template <typename T>
+__global__ void k_resort_count(Dev<T> d, KParams<T> kp, int bits, int tc, int tc_full) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * RESORT_UNROLL;
+  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31)) * RESORT_UNROLL; base < kp.n;
+       base += stride) {
+    uint32_t c[RESORT_UNROLL];
+    uint8_t f[RESORT_UNROLL];
+    T ox[RESORT_UNROLL], oy[RESORT_UNROLL], oz[RESORT_UNROLL], vx[RESORT_UNROLL], vy[RESORT_UNROLL], vz[RESORT_UNROLL];
+#pragma unroll
+    for (int u = 0; u < RESORT_UNROLL; ++u) {
+      const int64_t i = base + 32 * u + lane;
+      c[u] = 0u; f[u] = FLAG_INLIST;
+      ox[u] = oy[u] = oz[u] = vx[u] = vy[u] = vz[u] = (T)0;
+      if (i < kp.n) {
+        c[u] = d.p.cell[i]; f[u] = d.p.flag[i];
+        ox[u] = d.p.ox[i]; oy[u] = d.p.oy[i]; oz[u] = d.p.oz[i];
+        vx[u] = d.p.vx[i]; vy[u] = d.p.vy[i]; vz[u] = d.p.vz[i];
+      }
+    }
+    uint32_t r[RESORT_UNROLL];
+#pragma unroll
+    for (int u = 0; u < RESORT_UNROLL; ++u) {
+      if (f[u] & FLAG_HOME_SHELL) {
+        if (!chk((int64_t)c[u] < d.sh.cap, d.ctr, 130, c[u])) c[u] = 0;
+        c[u] = d.sh.cell[c[u]];
+      } else if (!(f[u] & FLAG_INLIST)) {
+        // the lag of k_rebuild / k_rebuild_far
+        const int lag = (f[u] & (FLAG_FRESH | FLAG_PASSIVE)) ? tc : tc_full;
+        if (lag > 0) {
+          uint8_t ff = f[u] & FLAG_SPECIES;
+          stream_one(kp, d.react_box, c[u], ox[u], oy[u], oz[u], vx[u], vy[u], vz[u], ff, true, lag);
+        }
+      }
+      uint32_t cid = unshifted_id(kp.lx, kp.ly, c[u]);
+      if (!chk(cid < (uint32_t)kp.ncell, d.ctr, 131, cid)) cid = 0;
+      r[u] = base + 32 * u + lane < kp.n ? d.order_rank[cid] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < RESORT_UNROLL; ++u) {
+      const int64_t i = base + 32 * u + lane;
+      const bool act = i < kp.n;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (!act) continue;
+      d.skey[i] = r[u];
+      const uint32_t b = r[u] >> bits;
+      const unsigned peers = __match_any_sync(am, b);
+      if (lane == __ffs(peers) - 1) atomicAdd(&d.scnt[b], (unsigned)__popc(peers));
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_resort_bin(Dev<T> d, KParams<T> kp, int bits) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * RESORT_UNROLL;
+  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31)) * RESORT_UNROLL; base < kp.n;
+       base += stride) {
+    uint32_t r[RESORT_UNROLL];
+#pragma unroll
+    for (int u = 0; u < RESORT_UNROLL; ++u) {
+      const int64_t i = base + 32 * u + lane;
+      r[u] = i < kp.n ? d.skey[i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < RESORT_UNROLL; ++u) {
+      const int64_t i = base + 32 * u + lane;
+      const bool act = i < kp.n;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (!act) continue;
+      const uint32_t b = r[u] >> bits;
+      const unsigned peers = __match_any_sync(am, b);
+      const int lead = __ffs(peers) - 1;
+      uint32_t pos = 0u;
+      if (lane == lead) pos = d.sstart[b] + atomicAdd(&d.sfill[b], (unsigned)__popc(peers));
+      pos = __shfl_sync(am, pos, lead);
+      const uint32_t q = pos + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+      if (!chk(q < (uint32_t)kp.n, d.ctr, 132, q)) continue;
+      d.sidx[q] = (uint32_t)i;
+      d.watch[q] = r[u];
+    }
+  }
+}
+
+// A particle's record in the main arrays (moved whole by the re-sort).
+template <typename T>
+struct Rec {
+  uint32_t cell, id;
+  T ox, oy, oz, vx, vy, vz;
+  uint8_t flag, inc;
+  uint16_t owner;
+};
+
+template <typename T>
+__device__ __forceinline__ Rec<T> rec_load(const Dev<T>& d, uint32_t i) {
+  Rec<T> r;
+  r.cell = d.p.cell[i];
+  r.ox = d.p.ox[i]; r.oy = d.p.oy[i]; r.oz = d.p.oz[i];
+  r.vx = d.p.vx[i]; r.vy = d.p.vy[i]; r.vz = d.p.vz[i];
+  r.flag = d.p.flag[i];
+  r.inc = d.inc ? d.inc[i] : 0;
+  r.owner = d.owner ? d.owner[i] : 0;
+  r.id = lid_of(d, i);
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ void rec_store(const Dev<T>& d, const Rec<T>& r, uint32_t q) {
+  d.p2.cell[q] = r.cell;
+  d.p2.ox[q] = r.ox; d.p2.oy[q] = r.oy; d.p2.oz[q] = r.oz;
+  d.p2.vx[q] = r.vx; d.p2.vy[q] = r.vy; d.p2.vz[q] = r.vz;
+  d.p2.flag[q] = r.flag;
+  if (d.inc) d.inc2[q] = r.inc;
+  if (d.owner) d.owner2[q] = r.owner;
+  d.lid2[q] = r.id;
+  d.lpos[r.id] = q;
+  if (r.flag & FLAG_HOME_SHELL) d.sh.idx[r.cell] = q;
+}
+
+// One block per bin (grid stride over the bins): the bin's (slot, rank)
+// list is staged in shared memory with coalesced loads, counted and ranked
+// there (a counting sort), and then the block writes the bin's new slots in
+// order (whole sectors), each thread gathering its records with all loads
+// in flight before the stores.
+template <typename T>
+__global__ void __launch_bounds__(TPB, 3) k_resort_fine(Dev<T> d, KParams<T> kp, int bits, int nbins) {
+  constexpr int PER = RESORT_CAP / TPB;   // members per thread
+  __shared__ uint32_t s_src[RESORT_CAP];
+  __shared__ uint16_t s_key[RESORT_CAP];
+  __shared__ uint32_t s_perm[RESORT_CAP];
+  __shared__ uint32_t s_off[1 << RESORT_MAX_BITS];
+  __shared__ uint32_t s_wsum[TPB / 32];
+  const int W = 1 << bits;
+  const uint32_t mask = (uint32_t)W - 1u;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = blockIdx.x; b < nbins; b += gridDim.x) {
+    const uint32_t start = d.sstart[b], n = d.scnt[b];
+    if (n > (uint32_t)RESORT_CAP) {
+      // (far above the mean) keep the bin order: still a valid permutation
+      for (uint32_t t = threadIdx.x; t < n; t += TPB) {
+        const uint32_t i = d.sidx[start + t];
+        if (chk(i < (uint32_t)kp.n, d.ctr, 134, (long long)i)) rec_store(d, rec_load(d, i), start + t);
+      }
+      __syncthreads();
+      continue;
+    }
+    if (threadIdx.x < W) s_off[threadIdx.x] = 0u;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t t = threadIdx.x + k * TPB;
+      if (t < n) { s_src[t] = d.sidx[start + t]; s_key[t] = (uint16_t)(d.watch[start + t] & mask); }
+    }
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < n; t += TPB) atomicAdd(&s_off[s_key[t]], 1u);
+    __syncthreads();
+    // exclusive scan of the W <= TPB counts
+    const uint32_t v = threadIdx.x < W ? s_off[threadIdx.x] : 0u;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t before = 0u;
+    for (int w = 0; w < warp; ++w) before += s_wsum[w];
+    if (threadIdx.x < W) s_off[threadIdx.x] = before + x - v;
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < n; t += TPB) s_perm[atomicAdd(&s_off[s_key[t]], 1u)] = s_src[t];
+    __syncthreads();
+    constexpr int G = 4;   // records in flight per thread
+#pragma unroll 1
+    for (int k0 = 0; k0 < PER; k0 += G) {
+      if (threadIdx.x + k0 * TPB >= n) break;
+      Rec<T> rec[G];
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        const uint32_t t = threadIdx.x + (k0 + k) * TPB;
+        if (t < n) {
+          const uint32_t i = s_perm[t];
+          if (chk(i < (uint32_t)kp.n, d.ctr, 135, (long long)i)) rec[k] = rec_load(d, i);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        const uint32_t t = threadIdx.x + (k0 + k) * TPB;
+        if (t < n) rec_store(d, rec[k], start + t);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+void Launch<T>::resort(Dev<T>& d, const KParams<T>& kp, int tc, int tc_full, cudaStream_t st) {
+  // bins of 2^bits ranks holding at most half the fine pass's capacity on average
+  const double per_cell = (double)kp.n / (double)kp.ncell;
+  int bits = 0;
+  while (bits < RESORT_MAX_BITS && (double)(2 << bits) * per_cell <= 0.5 * RESORT_CAP) ++bits;
+  const int nbins = (int)((kp.ncell + (1 << bits) - 1) >> bits);
+  cudaMemsetAsync(d.scnt, 0, sizeof(uint32_t) * nbins, st);
+  cudaMemsetAsync(d.sfill, 0, sizeof(uint32_t) * nbins, st);
+  k_resort_count<T><<<1024, TPB, 0, st>>>(d, kp, bits, tc, tc_full);
+  scan_u32(d.scnt, d.sstart, nbins, d.scan_tmp, st);
+  k_resort_bin<T><<<1024, TPB, 0, st>>>(d, kp, bits);
+  k_resort_fine<T><<<nbins < 65535 ? nbins : 65535, TPB, 0, st>>>(d, kp, bits, nbins);
+  LAUNCH_COUNT(); LAUNCH_COUNT(); LAUNCH_COUNT();
+  Particles<T> t = d.p; d.p = d.p2; d.p2 = t;
+  uint16_t* o = d.owner; d.owner = d.owner2; d.owner2 = o;
+  uint8_t* c = d.inc; d.inc = d.inc2; d.inc2 = c;
+  uint32_t* l = d.lid; d.lid = d.lid2; d.lid2 = l;
+}
+
 template <typename T>
 void Launch<T>::sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
   cudaMemsetAsync(d.scnt, 0, sizeof(uint32_t) * kp.ncell, st);
@@ -2695,6 +2958,8 @@ void Launch<T>::sort(Dev<T>& d, const KParams<T>& kp, cudaStream_t st) {
   Particles<T> t = d.p; d.p = d.p2; d.p2 = t;
   uint16_t* o = d.owner; d.owner = d.owner2; d.owner2 = o;
   uint8_t* c = d.inc; d.inc = d.inc2; d.inc2 = c;
+  // slot q now holds the particle the reference numbers q
+  if (d.lid) { d.lid2 = d.lid; d.lid = nullptr; d.lpos = nullptr; }
 }
 
 // --------------------------------------------------------------- reductions --
