@@ -843,6 +843,7 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
     for (int w = threadIdx.x; w < nmask; w += blockDim.x) smask[w] = d.bin_mask[w];
     __syncthreads();
   }
+  __shared__ uint32_t s_gmin[TPB];   // per-warp group minima of the main index (after a re-sort)
   __shared__ uint32_t wl_buf[(TPB / 32) * WL_CAP];
   uint32_t* wbuf = wl_buf + (threadIdx.x >> 5) * WL_CAP;
   unsigned wn = 0;
@@ -935,9 +936,20 @@ __global__ void __launch_bounds__(TPB, 4) k_rebuild_far(Dev<T> d, KParams<T> kp,
       unsigned peers = 0u;
       if (dist) peers = __match_any_sync(dmask, (cid << 2) | (uint32_t)sp);
       // the group's lowest lane holds its smallest index unless re-sorted
-      // slots put the indices out of order
+      // slots put the indices out of order; then the group's lanes take the
+      // minimum at their leader's slot of a per-warp table in shared memory
+      // (convergent; a reduction over each group's own mask serialises the
+      // groups and cost a sixth of the pass)
       uint32_t first_i = (uint32_t)i;
-      if (dist && d.lid) first_i = __reduce_min_sync(peers, my_lid);
+      if (d.lid) {
+        uint32_t* gmin = s_gmin + (threadIdx.x & ~31);
+        gmin[lane] = 0xFFFFFFFFu;
+        __syncwarp();
+        if (dist) atomicMin(&gmin[__ffs(peers) - 1], my_lid);
+        __syncwarp();
+        first_i = gmin[lane];
+        __syncwarp();
+      }
       if (dist && lane == __ffs(peers) - 1) {
         if (pend_cnt && ((pend_old >> pend_shift) & 255u) + pend_cnt > (unsigned)kp.cell_capacity)
           atomicOr(&d.ctr->status, DEV_ERR_CELL_OVERFLOW);
