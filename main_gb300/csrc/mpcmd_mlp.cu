@@ -5,19 +5,25 @@
 //
 // Every contraction (forward, input gradient, weight gradient) is one GEMM
 // form, C[M, N] = A[M, K] . B[N, K]^T with A and B BF16 and K-major, and one
-// kernel, k_gemm: per CTA a 128 x BN output tile; one thread streams the A and
-// B tiles into shared memory with TMA (cp.async.bulk.tensor, 128-byte
-// swizzle, a ring of STAGES stages on mbarriers); one thread issues
-// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor memory)
-// and releases each stage with tcgen05.commit; the four warps then read the
-// accumulator back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, one
-// row each) and apply the fused epilogue: bias + SiLU with the pre-activation
-// kept for the backward pass (forward hidden), bias (output), SiLU' of the
-// kept pre-activation (input gradient), or the FP32 weight gradient.  The
-// forms that the next GEMM needs transposed are written both ways, so that
-// every operand stays K-major.  Every mbarrier wait is bounded (two seconds
-// of globaltimer): on expiry the kernel raises an error flag, skips its
-// remaining work and still frees its tensor memory.
+// persistent kernel, k_gemm, with one CTA per SM walking its share of the
+// 128 x BN output tiles.  Warp roles: one thread streams the A and B tiles
+// into a ring of shared-memory stages with TMA (cp.async.bulk.tensor,
+// 128-byte swizzle, mbarriers); one thread issues tcgen05.mma (kind::f16,
+// BF16 operands, FP32 accumulator in tensor memory) and releases each stage
+// with tcgen05.commit; eight epilogue warps read the accumulator back with
+// tcgen05.ld (a warp reaches the 32 TMEM lanes of its quarter; two warps
+// share a quarter, one column half each) and apply the fused epilogue: bias
+// + SiLU with the pre-activation kept for the backward pass (forward
+// hidden), bias (output), SiLU' of the kept pre-activation (input
+// gradient), or the FP32 weight gradient.  Two accumulators in tensor
+// memory let the epilogue of one tile overlap the loads and MMAs of the
+// next.  Row-major outputs go through a per-warp 32 x 32 staging tile in
+// shared memory so that every store writes a row's contiguous columns; the
+// forms that the next GEMM needs transposed are also written from the
+// thread-per-row layout, so that every operand stays K-major.  Every
+// mbarrier wait is bounded (two seconds of globaltimer): on expiry the
+// kernel raises an error flag, skips its remaining work, waits for its
+// copies and MMAs in flight and still frees its tensor memory.
 //
 // Weights are kept in FP32 (master copy for Adam) and in BF16 twice: [N, K]
 // for the forward GEMM and [K, N] for the input-gradient GEMM.
@@ -35,11 +41,13 @@
 
 namespace {
 
-constexpr int BM = 128;        // output rows per CTA (the MMA's M)
+constexpr int BM = 128;        // output rows per tile (the MMA's M)
 constexpr int BK = 64;         // K per stage: one 128-byte swizzle row of BF16
-constexpr int STAGES = 4;
-constexpr int THREADS = 128;
+constexpr int EPI_WARPS = 16;                 // four per TMEM lane quarter
+constexpr int THREADS = 64 + 32 * EPI_WARPS;   // producer warp, MMA warp, epilogue warps
 constexpr int A_STAGE = BM * BK * 2;   // 16 KiB
+template <int BN>
+__host__ __device__ constexpr int stages() { return BN == 256 ? 3 : 4; }
 
 enum Epilogue : int { EP_HIDDEN = 0, EP_HIDDEN_INFER = 1, EP_OUT = 2, EP_DX = 3, EP_DW = 4 };
 
@@ -134,51 +142,205 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 }
 __device__ __forceinline__ void tmem_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tmem_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ float sigm(float z) { return 1.f / (1.f + expf(-z)); }
+// SiLU and its derivative with the fast exponential and division: the
+// results are rounded to BF16 right after.
+__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+__device__ __forceinline__ float dsilu_f(float z) {
+  const float s = __frcp_rn(1.f + __expf(-z));
+  return s * (1.f + z * (1.f - s));
+}
+
+// Row-major store of a warp's 32-row block (thread = row, W 32-bit words
+// per row) through the warp's staging tile: the block is written in the
+// thread-per-row layout and read back so that each lane carries VB
+// consecutive bytes of one row and each store instruction writes whole rows
+// (full sectors), rows from `row0` of `base` with pitch `pitch` bytes.
+constexpr int STAGE_PITCH = 36;   // words per staging row (16-byte rows, conflict-free quarter warps)
+
+template <int W, int VB>
+__device__ __forceinline__ void store_rows(uint32_t* buf, const uint32_t (&w)[W], int lane, char* base, int row0,
+                                           size_t pitch, int rows, int wlim = W) {
+  static_assert(W % 4 == 0 && (VB == 16 || VB == 8 || VB == 4), "staged row store shape");
+#pragma unroll
+  for (int q = 0; q < W; q += 4)
+    *reinterpret_cast<uint4*>(buf + lane * STAGE_PITCH + q) = make_uint4(w[q], w[q + 1], w[q + 2], w[q + 3]);
+  __syncwarp();
+  constexpr int LPR = W * 4 / VB;    // lanes per row
+  constexpr int RPI = 32 / LPR;      // rows per instruction
+  const int sub = lane / LPR, q = lane % LPR;
+  const int w0 = q * (VB / 4);       // first word of this lane's piece
+#pragma unroll 4
+  for (int it = 0; it < 32 / RPI; ++it) {
+    const int r = it * RPI + sub;
+    if (r < rows && w0 < wlim) {
+      char* dst = base + (size_t)(row0 + r) * pitch + q * VB;
+      const uint32_t* src = buf + r * STAGE_PITCH + w0;
+      if (w0 + VB / 4 <= wlim) {
+        if (VB == 16) *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
+        else if (VB == 8) *reinterpret_cast<uint2*>(dst) = *reinterpret_cast<const uint2*>(src);
+        else *reinterpret_cast<uint32_t*>(dst) = *src;
+      } else {
+        for (int k = 0; w0 + k < wlim; ++k) reinterpret_cast<uint32_t*>(dst)[k] = src[k];
+      }
+    }
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&p);
+}
+
+// Epilogue of a warp's 32 x 32 block: rows row0.. (this thread: row0 +
+// lane), columns n..n+31, accumulators v[] in the tcgen05.ld 32x32b layout
+// (lane = row, registers = consecutive columns).  The arithmetic runs in that
+// layout; row-major outputs leave through store_rows, the transposed copies
+// as one BF16 per lane and column (consecutive lanes = consecutive rows).
+template <int MODE>
+__device__ __forceinline__ void epilogue_chunk(const GemmArgs& a, uint32_t* buf, const float (&v)[32], int row0,
+                                               int n, int rows, int lane) {
+  const int m = row0 + lane;
+  const bool row_ok = lane < rows;
+  // bias, four columns at a time (the same address in every lane)
+  const float4* bp = reinterpret_cast<const float4*>(a.bias + n);
+  switch (MODE) {
+    case EP_HIDDEN:
+    case EP_HIDDEN_INFER: {
+      uint32_t zw[32], hw[16];
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        const float4 b4 = bp[q / 4];
+        zw[q] = __float_as_uint(v[q] + b4.x); zw[q + 1] = __float_as_uint(v[q + 1] + b4.y);
+        zw[q + 2] = __float_as_uint(v[q + 2] + b4.z); zw[q + 3] = __float_as_uint(v[q + 3] + b4.w);
+      }
+      if (MODE == EP_HIDDEN)
+        store_rows<32, 16>(buf, zw, lane, reinterpret_cast<char*>(a.z + n), row0, (size_t)a.ldz * 4, rows);
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        hw[q] = pack_bf16(silu_f(__uint_as_float(zw[2 * q])), silu_f(__uint_as_float(zw[2 * q + 1])));
+      if (MODE == EP_HIDDEN) {
+        if (row_ok) {
+          const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(hw);
+#pragma unroll
+          for (int q = 0; q < 32; ++q) a.out_t[(size_t)(n + q) * a.ldt + m] = h[q];
+        }
+      }
+      store_rows<16, 16>(buf, hw, lane, reinterpret_cast<char*>(a.out_bf16 + n), row0, (size_t)a.ldb * 2, rows);
+      break;
+    }
+    case EP_OUT: {
+      uint32_t yw[32];
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        const float4 b4 = bp[q / 4];
+        yw[q] = __float_as_uint(v[q] + b4.x); yw[q + 1] = __float_as_uint(v[q + 1] + b4.y);
+        yw[q + 2] = __float_as_uint(v[q + 2] + b4.z); yw[q + 3] = __float_as_uint(v[q + 3] + b4.w);
+      }
+      // y rows have the caller's pitch: pieces as wide as its alignment allows
+      const int wlim = a.n_valid - n < 32 ? a.n_valid - n : 32;
+      char* yb = reinterpret_cast<char*>(a.out_f32 + n);
+      if ((a.ldo & 3) == 0) store_rows<32, 16>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
+      else if ((a.ldo & 1) == 0) store_rows<32, 8>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
+      else store_rows<32, 4>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
+      break;
+    }
+    case EP_DW: {
+      uint32_t gw[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) gw[q] = __float_as_uint(v[q]);
+      store_rows<32, 16>(buf, gw, lane, reinterpret_cast<char*>(a.out_f32 + n), row0, (size_t)a.ldo * 4, rows);
+      break;
+    }
+    case EP_DX: {
+      uint32_t gw[16];
+      if (row_ok) {
+        const float4* zp = reinterpret_cast<const float4*>(a.z + (size_t)m * a.ldz + n);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float4 z4 = zp[q];
+          gw[2 * q] = pack_bf16(v[4 * q] * dsilu_f(z4.x), v[4 * q + 1] * dsilu_f(z4.y));
+          gw[2 * q + 1] = pack_bf16(v[4 * q + 2] * dsilu_f(z4.z), v[4 * q + 3] * dsilu_f(z4.w));
+        }
+        const __nv_bfloat16* g = reinterpret_cast<const __nv_bfloat16*>(gw);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) a.out_t[(size_t)(n + q) * a.ldt + m] = g[q];
+      } else {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) gw[q] = 0u;
+      }
+      store_rows<16, 16>(buf, gw, lane, reinterpret_cast<char*>(a.out_bf16 + n), row0, (size_t)a.ldb * 2, rows);
+      break;
+    }
+  }
+}
 
 // ------------------------------------------------------------ GEMM ----
 template <int BN>
+__host__ __device__ constexpr size_t gemm_smem_bytes() {
+  return 1024 + (size_t)stages<BN>() * (A_STAGE + BN * BK * 2) + (size_t)EPI_WARPS * 32 * STAGE_PITCH * 4 +
+         (2 * stages<BN>() + 5) * 8 + 16;
+}
+
+template <int BN, int MODE>
 __global__ void __launch_bounds__(THREADS, 1)
     k_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmArgs a) {
+  constexpr int S = stages<BN>();
   constexpr int B_STAGE = BN * BK * 2;
-  static_assert(BM * (BN + 1) * 4 <= STAGES * (A_STAGE + B_STAGE), "the staged epilogue tile fits the stage ring");
+  static_assert(gemm_smem_bytes<BN>() <= 232448, "shared memory of one CTA");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = smem;
-  uint8_t* sB = smem + STAGES * A_STAGE;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + STAGES * B_STAGE);   // full[S], empty[S], done
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
-  __shared__ int bail;   // a wait of this CTA expired
+  uint8_t* sB = smem + S * A_STAGE;
+  uint32_t* stage_all = reinterpret_cast<uint32_t*>(sB + S * B_STAGE);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stage_all + EPI_WARPS * 32 * STAGE_PITCH);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 5);
+  __shared__ volatile int bail;        // a wait of this CTA expired
+  __shared__ int issued;               // stage loads the producer issued
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int tiles_n = a.N / BN, tiles = ((a.M + BM - 1) / BM) * tiles_n;
   const int nk = a.K / BK;
-  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), done = smem_u32(bars + 2 * STAGES);
+  const int mlim = (MODE == EP_OUT || MODE == EP_DW) ? a.m_valid : a.M;
+  // barriers: full[S], empty[S] (stage ring), accf[2], acce[2] (accumulators), done
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), accf0 = smem_u32(bars + 2 * S),
+                 acce0 = smem_u32(bars + 2 * S + 2), done = smem_u32(bars + 2 * S + 4);
 
   if (threadIdx.x == 0) {
     bail = 0;
-    for (int s = 0; s < STAGES; ++s) {
+    issued = 0;
+    for (int s = 0; s < S; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, EPI_WARPS);
     }
     mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(BN)
+                 "r"(2 * BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -187,123 +349,87 @@ __global__ void __launch_bounds__(THREADS, 1)
   tmem_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0 && lane == 0) {
-    // TMA producer
-    for (int k = 0; k < nk; ++k) {
-      const int s = k % STAGES;
-      const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
-      if (k >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1u, a.err)) { bail = 1; break; }
-      mbar_expect_tx(full0 + 8 * s, A_STAGE + B_STAGE);
-      tma_load_2d(smem_u32(sA + s * A_STAGE), &ta, full0 + 8 * s, k * BK, m0);
-      tma_load_2d(smem_u32(sB + s * B_STAGE), &tb, full0 + 8 * s, k * BK, n0);
+  if (warp == 0) {
+    if (lane == 0) {
+      // TMA producer
+      int g = 0;
+      for (int t = blockIdx.x; t < tiles && !bail; t += gridDim.x) {
+        const int m0 = (t / tiles_n) * BM, n0 = (t % tiles_n) * BN;
+        for (int k = 0; k < nk; ++k) {
+          const int s = g % S;
+          if (g >= S && !mbar_wait(empty0 + 8 * s, ((uint32_t)(g / S) & 1u) ^ 1u, a.err)) { bail = 1; break; }
+          mbar_expect_tx(full0 + 8 * s, A_STAGE + B_STAGE);
+          tma_load_2d(smem_u32(sA + s * A_STAGE), &ta, full0 + 8 * s, k * BK, m0);
+          tma_load_2d(smem_u32(sB + s * B_STAGE), &tb, full0 + 8 * s, k * BK, n0);
+          ++g;
+        }
+      }
+      issued = g;
     }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    constexpr uint32_t idesc = f16_idesc(BM, BN);
-    bool ok = true;
-    for (int k = 0; k < nk; ++k) {
-      const int s = k % STAGES;
-      const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
-      if (!mbar_wait(full0 + 8 * s, ph, a.err)) { ok = false; bail = 1; break; }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer: tile j accumulates into buffer j & 1
+      constexpr uint32_t idesc = f16_idesc(BM, BN);
+      int g = 0, j = 0;
+      for (int t = blockIdx.x; t < tiles && !bail; t += gridDim.x, ++j) {
+        const int b = j & 1;
+        if (j >= 2 && !mbar_wait(acce0 + 8 * b, ((uint32_t)(j >> 1) & 1u) ^ 1u, a.err)) { bail = 1; break; }
+        tmem_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * BN);
+        bool ok = true;
+        for (int k = 0; k < nk; ++k, ++g) {
+          const int s = g % S;
+          if (!mbar_wait(full0 + 8 * s, (uint32_t)(g / S) & 1u, a.err)) { ok = false; bail = 1; break; }
+          tmem_fence_after();
+          const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk)
+            mma_bf16(acc, sw128_desc(a0 + 32 * kk), sw128_desc(b0 + 32 * kk), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+          mma_commit(empty0 + 8 * s);
+        }
+        if (!ok) break;
+        mma_commit(accf0 + 8 * b);   // arrives when the tile's MMAs have completed
+      }
+      mma_commit(done);   // arrives when every MMA issued above has completed
+    }
+  } else {
+    // epilogue: warp w reaches TMEM lanes 32 (w % 4) ..; the warps of a
+    // quarter take its 32-column chunks in turn
+    const int ew = warp - 2;
+    const int quarter = warp & 3;
+    constexpr int GROUPS = EPI_WARPS / 4;
+    int j = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++j) {
+      const int b = j & 1;
+      if (!mbar_wait(accf0 + 8 * b, (uint32_t)(j >> 1) & 1u, a.err)) { bail = 1; break; }
       tmem_fence_after();
-      const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
-#pragma unroll
-      for (int kk = 0; kk < BK / 16; ++kk)
-        mma_bf16(tmem, sw128_desc(a0 + 32 * kk), sw128_desc(b0 + 32 * kk), idesc, (k > 0 || kk > 0) ? 1u : 0u);
-      mma_commit(empty0 + 8 * s);
+      const int row0 = (t / tiles_n) * BM + quarter * 32, n0 = (t % tiles_n) * BN;
+      const int rows = mlim - row0 < 32 ? mlim - row0 : 32;
+      uint32_t* buf = stage_all + ew * 32 * STAGE_PITCH;
+      for (int c0 = (ew >> 2) * 32; c0 < BN; c0 += 32 * GROUPS) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN + c0), v);
+        epilogue_chunk<MODE>(a, buf, v, row0, n0 + c0, rows, lane);
+      }
+      tmem_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce0 + 8 * b);
     }
-    (void)ok;
-    mma_commit(done);   // arrives when every MMA issued above has completed
   }
-  // every copy and MMA of this CTA is issued (and `bail` is visible); the
-  // done barrier tracks every MMA issued, so it is always waited for before
-  // the tensor memory is read or freed
   __syncthreads();
-  const bool done_ok = mbar_wait(done, 0, a.err);
-  const bool have = __syncthreads_and(done_ok && !bail) != 0;   // uniform over the CTA
-  // epilogue: warp w owns accumulator rows 32w..32w+31
-  tmem_fence_after();
-  const int m = m0 + warp * 32 + lane;
-  const bool staged = a.mode == EP_OUT || a.mode == EP_DW || a.mode == EP_HIDDEN_INFER;
-  if (staged) {
-    // Row-major outputs without a transposed copy go through shared memory:
-    // thread = row in tensor memory, so direct stores would write 32 rows
-    // per instruction; staged, a warp writes one row's contiguous columns.
-    // The tile (128 x (BN + 1) floats, the odd stride keeps both phases free
-    // of bank conflicts) reuses the drained stage ring.
-    float* tile = reinterpret_cast<float*>(smem);
-    constexpr int LD = BN + 1;
-    if (have) {
-      const int r = warp * 32 + lane;
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        const int nb = n0 + c0;
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          float o = v[q];
-          if (a.mode != EP_DW) o += a.bias[nb + q];
-          if (a.mode == EP_HIDDEN_INFER) o = o * sigm(o);
-          tile[r * LD + c0 + q] = o;
-        }
-      }
-    }
-    __syncthreads();
-    if (have) {
-      for (int r = warp; r < BM; r += THREADS / 32) {
-        const int mm = m0 + r;
-        if (a.mode != EP_HIDDEN_INFER && mm >= a.m_valid) continue;
-        for (int c = lane; c < BN; c += 32) {
-          const int n = n0 + c;
-          const float o = tile[r * LD + c];
-          if (a.mode == EP_HIDDEN_INFER) a.out_bf16[(size_t)mm * a.ldb + n] = __float2bfloat16_rn(o);
-          else if (a.mode == EP_DW || n < a.n_valid) a.out_f32[(size_t)mm * a.ldo + n] = o;
-        }
-      }
-    }
-  } else if (have) {
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      const int nb = n0 + c0;
-      switch (a.mode) {
-        case EP_HIDDEN: {
-          __align__(16) __nv_bfloat16 h[16];
-#pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const float z = v[q] + a.bias[nb + q];
-            a.z[(size_t)m * a.ldz + nb + q] = z;
-            h[q] = __float2bfloat16_rn(z * sigm(z));
-          }
-          uint4* dst = reinterpret_cast<uint4*>(a.out_bf16 + (size_t)m * a.ldb + nb);
-          dst[0] = reinterpret_cast<const uint4*>(h)[0];
-          dst[1] = reinterpret_cast<const uint4*>(h)[1];
-#pragma unroll
-          for (int q = 0; q < 16; ++q) a.out_t[(size_t)(nb + q) * a.ldt + m] = h[q];
-          break;
-        }
-        case EP_DX: {
-          __align__(16) __nv_bfloat16 g[16];
-#pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const float z = a.z[(size_t)m * a.ldz + nb + q];
-            const float s = sigm(z);
-            g[q] = __float2bfloat16_rn(v[q] * (s * (1.f + z * (1.f - s))));
-          }
-          uint4* dst = reinterpret_cast<uint4*>(a.out_bf16 + (size_t)m * a.ldb + nb);
-          dst[0] = reinterpret_cast<const uint4*>(g)[0];
-          dst[1] = reinterpret_cast<const uint4*>(g)[1];
-#pragma unroll
-          for (int q = 0; q < 16; ++q) a.out_t[(size_t)(nb + q) * a.ldt + m] = g[q];
-          break;
-        }
-      }
-    }
+  if (threadIdx.x == 0) {
+    // every MMA has completed, and so has every stage load that was issued
+    // (the most recent phase of each stage; on the normal path all were
+    // consumed), before the tensor memory is freed and the CTA exits
+    mbar_wait(done, 0, a.err);
+    const int g1 = issued;
+    for (int g = g1 - S < 0 ? 0 : g1 - S; g < g1; ++g) mbar_wait(full0 + 8 * (g % S), (uint32_t)(g / S) & 1u, a.err);
   }
   tmem_fence_before();
   __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  tmem_fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
 }
 
 // ------------------------------------------------------- small kernels ----
@@ -413,11 +539,6 @@ bool make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, in
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int BN>
-size_t gemm_smem() {
-  return (size_t)STAGES * (A_STAGE + BN * BK * 2) + (2 * STAGES + 1) * 8 + 16 + 1024;
-}
-
 struct Layer {
   int n, k;               // padded output and input widths: W [n, k]
   int n_real, k_real;     // logical widths
@@ -441,6 +562,7 @@ struct mpcmd_mlp {
   double* dloss = nullptr;
   int* derr = nullptr;
   int64_t step = 0;
+  int sms = 1;             // SMs of the device (one persistent GEMM CTA each)
   cudaStream_t st = nullptr;
 
   ~mpcmd_mlp() {
@@ -467,6 +589,42 @@ int status_of(mpcmd_mlp* m) {
   return e ? MPCMD_ERR_CUDA : MPCMD_OK;
 }
 
+// One persistent CTA per SM (at most one per tile).
+template <int BN, int MODE>
+void launch_one(mpcmd_mlp* m, int grid, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g) {
+  k_gemm<BN, MODE><<<grid, THREADS, gemm_smem_bytes<BN>(), m->st>>>(ta, tb, g);
+}
+
+template <int BN>
+void launch_bn(mpcmd_mlp* m, int grid, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g) {
+  switch (g.mode) {
+    case EP_HIDDEN: launch_one<BN, EP_HIDDEN>(m, grid, ta, tb, g); break;
+    case EP_HIDDEN_INFER: launch_one<BN, EP_HIDDEN_INFER>(m, grid, ta, tb, g); break;
+    case EP_OUT: launch_one<BN, EP_OUT>(m, grid, ta, tb, g); break;
+    case EP_DX: launch_one<BN, EP_DX>(m, grid, ta, tb, g); break;
+    default: launch_one<BN, EP_DW>(m, grid, ta, tb, g); break;
+  }
+}
+
+template <int BN>
+bool allow_smem() {
+  const int b = (int)gemm_smem_bytes<BN>();
+  return cudaFuncSetAttribute(k_gemm<BN, EP_HIDDEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+         cudaFuncSetAttribute(k_gemm<BN, EP_HIDDEN_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+         cudaFuncSetAttribute(k_gemm<BN, EP_OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+         cudaFuncSetAttribute(k_gemm<BN, EP_DX>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+         cudaFuncSetAttribute(k_gemm<BN, EP_DW>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess;
+}
+
+int launch_gemm(mpcmd_mlp* m, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g, int BN) {
+  const int tiles = ((g.M + BM - 1) / BM) * (g.N / BN);
+  const int grid = tiles < m->sms ? tiles : m->sms;
+  if (BN == 256) launch_bn<256>(m, grid, ta, tb, g);
+  else if (BN == 128) launch_bn<128>(m, grid, ta, tb, g);
+  else launch_bn<64>(m, grid, ta, tb, g);
+  return cudaPeekAtLastError() == cudaSuccess ? MPCMD_OK : MPCMD_ERR_CUDA;
+}
+
 // C[M, N] = A[M, K] . B[N, K]^T on tcgen05; A and B row-major BF16 with
 // A_rows x K and B_rows x K allocated (K-major), M, N tile multiples.
 int gemm(mpcmd_mlp* m, const void* A, int64_t a_rows, const void* Bm, int64_t b_rows, int M, int N, int K, GemmArgs g,
@@ -474,11 +632,7 @@ int gemm(mpcmd_mlp* m, const void* A, int64_t a_rows, const void* Bm, int64_t b_
   CUtensorMap ta, tb;
   if (!make_map(&ta, A, a_rows, K, BM) || !make_map(&tb, Bm, b_rows, K, BN)) return MPCMD_ERR_CUDA;
   g.M = M; g.N = N; g.K = K; g.err = m->derr;
-  dim3 grid(M / BM, N / BN);
-  if (BN == 256) k_gemm<256><<<grid, THREADS, gemm_smem<256>(), m->st>>>(ta, tb, g);
-  else if (BN == 128) k_gemm<128><<<grid, THREADS, gemm_smem<128>(), m->st>>>(ta, tb, g);
-  else k_gemm<64><<<grid, THREADS, gemm_smem<64>(), m->st>>>(ta, tb, g);
-  return cudaPeekAtLastError() == cudaSuccess ? MPCMD_OK : MPCMD_ERR_CUDA;
+  return launch_gemm(m, ta, tb, g, BN);
 }
 
 int pick_bn(int N) { return N % 256 == 0 ? 256 : (N % 128 == 0 ? 128 : 64); }
@@ -535,13 +689,8 @@ int backward(mpcmd_mlp* m, const float* x, const float* t, const float* w) {
     CUtensorMap ta, tb;
     if (!make_map(&ta, gt, ly.n, gt_pitch, BM) || !make_map(&tb, xin_t, ly.k, m->R, pick_bn(ly.k))) return MPCMD_ERR_CUDA;
     g.M = ly.n; g.N = ly.k; g.K = B; g.err = m->derr;
-    {
-      const int BN = pick_bn(ly.k);
-      dim3 grid(ly.n / BM, ly.k / BN);
-      if (BN == 256) k_gemm<256><<<grid, THREADS, gemm_smem<256>(), m->st>>>(ta, tb, g);
-      else if (BN == 128) k_gemm<128><<<grid, THREADS, gemm_smem<128>(), m->st>>>(ta, tb, g);
-      else k_gemm<64><<<grid, THREADS, gemm_smem<64>(), m->st>>>(ta, tb, g);
-    }
+    r = launch_gemm(m, ta, tb, g, pick_bn(ly.k));
+    if (r) return r;
     k_rowsum<<<(ly.n * 32 + 255) / 256, 256, 0, m->st>>>(gt, ly.n, (int)gt_pitch, B, ly.gb);
     if (l == 0) break;
     // input gradient through W and SiLU' of the previous layer's pre-activation
@@ -669,9 +818,10 @@ int mpcmd_mlp_create(const mpcmd_mlp_config* cfg, mpcmd_mlp** out) {
   s |= m->alloc(m->dloss, 1);
   s |= m->alloc(m->derr, 1);
   if (s) { delete m; return MPCMD_ERR_ALLOC; }
-  if (cudaFuncSetAttribute(k_gemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<256>()) ||
-      cudaFuncSetAttribute(k_gemm<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<128>()) ||
-      cudaFuncSetAttribute(k_gemm<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<64>())) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      !allow_smem<256>() || !allow_smem<128>() || !allow_smem<64>()) {
     delete m;
     return MPCMD_ERR_CUDA;
   }
