@@ -316,12 +316,18 @@ def gpu_arm(args, ws, rk, lr, dist):
         barrier()
         t0 = time.perf_counter()
         e.upload_state(host)
+        tu = time.perf_counter()
         e.prepare()
+        e.synchronize()
+        tp = time.perf_counter()
         for _ in range(args.steps):
             e.run(S)
             e.observables()
+        tl = time.perf_counter()
         e.download_state(out=host)   # into the same page-locked buffers
         t1 = time.perf_counter()
+        phases = {"upload": round(tu - t0, 4), "prepare": round(tp - tu, 4), "periods": round(tl - tp, 4),
+                  "download": round(t1 - tl, 4)}
         state_bytes = N * (6 * 8 + 4) + ns * 3 * 8 * 3
         obs_bytes = 8 * 16 + ns * 3 * 8 + cfg["n_dimers"] * 8
         e2e_s = t1 - t0
@@ -329,7 +335,7 @@ def gpu_arm(args, ws, rk, lr, dist):
         e2e = {"value": aggregate_rate(ws, N, S, args.steps, e2e_s), "unit": UNIT,
                "h2d_bytes_per_step": int(state_bytes / args.steps),
                "d2h_bytes_per_step": int((state_bytes + args.steps * obs_bytes) / args.steps),
-               "pinned_host": pinned,
+               "pinned_host": pinned, "phases_s": phases,
                "what": "upload of the full host state, prepare, %d x (collision period + observables), download "
                        "of the full host state" % args.steps}
     return dict(value=value, ms=ms, launches=launches, clocks=clocks, roofline=roofline, e2e=e2e, cfg=cfg,
@@ -518,10 +524,10 @@ def main_surrogate(args, ws, rk, lr):
             "--periods", str(args.periods), "--epochs", str(args.epochs)]
     out = sweep.main(argv)
     try:
-        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"])
-        peak_kind = "measured"
+        pk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, hbm, peak_kind = float(pk["bf16_tflops"]), float(pk["hbm_gbs"]), "measured"
     except Exception:
-        peak, peak_kind = 1900.0, "fallback"
+        peak, hbm, peak_kind = 1900.0, 6800.0, "fallback"
     inf = out["inference"]
     sw = out["sweep"]
     line = {"metric": METRIC, "value": sw["speedup_vs_single_context"], "unit": "x (sweep time plain / surrogate)",
@@ -532,9 +538,17 @@ def main_surrogate(args, ws, rk, lr):
                                    "accumulation, trained on %d batched-ensemble replicas (Adam, lr 1e-3, batch 256); "
                                    "%d-point sweep screened with plain-simulation fallback; %d collision periods per "
                                    "run" % (args.train, args.sweep, args.periods), "name": "c4"},
-            "roofline": {"bound": "tensor", "kernel": "k_gemm (forward of %d points)" % inf["points"],
-                         "achieved": round(inf["tflops"], 2), "peak": peak, "peak_source": peak_kind,
-                         "unit": "TFLOP/s", "frac": round(inf["tflops"] / peak, 4), "traffic": None},
+            # at K = 256 the forward pass moves more bytes than the tensor
+            # cores need time for (the FP32 output alone is 537 MB at 65,536
+            # points): its binding roofline is HBM; the tensor fraction is
+            # given beside it
+            "roofline": {"bound": "hbm", "kernel": "k_gemm (forward of %d points, five launches)" % inf["points"],
+                         "achieved": round(inf["gbs"], 1), "peak": hbm, "peak_source": peak_kind,
+                         "unit": "GB/s", "frac": round(inf["gbs"] / hbm, 4), "traffic": None,
+                         "algorithmic_bytes_per_launch": int(inf["bytes"]),
+                         "what": "inputs, BF16 activations written and read once, weights, FP32 outputs",
+                         "tensor": {"achieved": round(inf["tflops"], 2), "peak": peak, "unit": "TFLOP/s",
+                                    "frac": round(inf["tflops"] / peak, 4)}},
             "surrogate": out}
     print(json.dumps(line))
     return 0

@@ -191,9 +191,18 @@ def main(argv=None):
     predict(net, sc, X_inf, cols=2)
     t_host = time.perf_counter() - t0
     ms = forward_device_ms(net, sc, X_inf)
-    flops = 2.0 * len(X_inf) * sum(n * k for n, k in net.shapes())
-    out["inference"] = {"points": len(X_inf), "seconds_with_host": t_host, "device_ms": ms,
-                        "tflops": flops / (ms * 1e-3) / 1e12, "flops": flops}
+    rows = len(X_inf)
+    shapes = net.shapes()
+    flops = 2.0 * rows * sum(n * k for n, k in shapes)
+    # the bytes a forward pass cannot avoid: the FP32 inputs (and their BF16
+    # 64-column copy written and read), every BF16 activation written once and
+    # read once, the BF16 weights, and the FP32 outputs
+    hidden = [n for n, _ in shapes[:-1]]
+    nbytes = (rows * shapes[0][1] * 4 + 2 * rows * 64 * 2 + sum(2 * rows * h * 2 for h in hidden)
+              + sum(n * k * 2 for n, k in shapes) + rows * shapes[-1][0] * 4)
+    out["inference"] = {"points": rows, "seconds_with_host": t_host, "device_ms": ms,
+                        "tflops": flops / (ms * 1e-3) / 1e12, "flops": flops,
+                        "bytes": nbytes, "gbs": nbytes / (ms * 1e-3) / 1e9}
 
     # the sweep: surrogate screen + plain fallback, against plain simulation of every point
     reps_sw = E.sample_replicas(a.sweep, seed=14, base_seed=30_000, wide=True)
