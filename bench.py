@@ -218,6 +218,8 @@ def gpu_arm(args, ws, rk, lr, dist):
     S = cfg["mpc_every"]
     N = cfg["n_solvent"]
     e = Engine(cfg)
+    if args.resort is not None:
+        e.set_resort(args.resort * S)
     e.initial()
     e.prepare()
     e.run(args.warmup * S)
@@ -574,6 +576,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-full", action="store_true", help="skip the full-size CPU period")
     ap.add_argument("--no-whole-run", action="store_true", help="skip the whole-run mean period time")
+    ap.add_argument("--resort", type=int, default=None,
+                    help="collision periods between order-only re-sorts (0: none; default: the engine's)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
