@@ -98,7 +98,18 @@ class Clocks:
                  "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
-        time.sleep(0.3)
+        # the timed region starts after the first sample: nvidia-smi's own
+        # start-up can hold the driver for a good part of a second, which
+        # would land inside a short timed region
+        t0 = time.time()
+        while self.proc is not None and time.time() - t0 < 10.0:
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.05)
+        time.sleep(0.1)
         return self
 
     def __exit__(self, *a):
