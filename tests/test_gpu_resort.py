@@ -101,3 +101,57 @@ def test_resort_interval_must_be_a_multiple_of_the_collision_interval():
     e.prepare()
     e.run(2 * cfg["mpc_every"])
     assert e.counters()["resorts"] == 0
+
+
+def test_resort_of_a_crowded_region_matches_oracle_fp64():
+    """Particles crowded into one corner of the box (density 60 in an 8^3
+    block, about 3 elsewhere): rank bins there hold more members than the
+    re-sort's shared-memory counting sort takes, so those bins keep their
+    bin order (the fallback path); the run still follows the oracle."""
+    import numpy as np
+    from main_gb300 import Engine
+    from oracle.oracle import Oracle
+    cfg = config.base_config(lx=16, ly=16, lz=16, n_dimers=0, n_solvent=40960, precision=64, cell_capacity=200)
+    rng = np.random.default_rng(17)
+    n_dense = 30720
+    pos = np.empty((cfg["n_solvent"], 3))
+    pos[:n_dense] = rng.random((n_dense, 3)) * 8.0
+    rest = []
+    while len(rest) < cfg["n_solvent"] - n_dense:
+        p = rng.random(3) * 16.0
+        if not (p < 8.0).all():
+            rest.append(p)
+    pos[n_dense:] = np.array(rest)
+    v = rng.normal(scale=np.sqrt(cfg["kT"]), size=pos.shape)
+    st = dict(x=pos[:, 0].copy(), y=pos[:, 1].copy(), z=pos[:, 2].copy(),
+              vx=v[:, 0].copy(), vy=v[:, 1].copy(), vz=v[:, 2].copy(),
+              flag=np.zeros(cfg["n_solvent"], np.int32),
+              dpos=np.zeros((0, 3)), dvel=np.zeros((0, 3)), dforce=np.zeros((0, 3)))
+    o = Oracle(cfg)
+    o.set_state(st)
+    e = Engine(cfg)
+    e.upload_state(st)
+    o.set_cell_order(e.cell_order())
+    e.set_resort(cfg["mpc_every"])
+    o.prepare()
+    e.prepare()
+    for chunk in (50, 70):
+        o.run(chunk)
+        e.run(chunk)
+        assert_close(e.download_state(), o.get_state(), cfg, pos=1e-9, vel=1e-9, flags=1.0)
+    assert e.counters()["resorts"] == 2
+
+
+@pytest.mark.parametrize("case", ["c0", "c2"])
+def test_resort_every_collision_fp32_trajectory(case):
+    """The FP32 production build with a re-sort at every collision step
+    follows the oracle within the FP32 trajectory bar of test_gpu_parity."""
+    cfg = CASES[case](32)
+    o, e = pair(cfg)
+    e.set_resort(cfg["mpc_every"])
+    o.prepare()
+    e.prepare()
+    o.run(120)
+    e.run(120)
+    assert e.counters()["resorts"] == 2
+    assert_close(e.download_state(), o.get_state(), cfg, pos=2e-4, vel=2e-3, flags=0.999, dimer=1e-4)
