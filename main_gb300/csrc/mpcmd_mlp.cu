@@ -46,10 +46,38 @@ constexpr int BK = 64;         // K per stage: one 128-byte swizzle row of BF16
 constexpr int EPI_WARPS = 16;                 // four per TMEM lane quarter
 constexpr int THREADS = 64 + 32 * EPI_WARPS;   // producer warp, MMA warp, epilogue warps
 constexpr int A_STAGE = BM * BK * 2;   // 16 KiB
-template <int BN>
-__host__ __device__ constexpr int stages() { return BN == 256 ? 3 : 4; }
+constexpr int K_MAX = 256;             // the longest K (hidden width) a resident operand holds
 
 enum Epilogue : int { EP_HIDDEN = 0, EP_HIDDEN_INFER = 1, EP_OUT = 2, EP_DX = 3, EP_DW = 4 };
+
+// Operand kept in shared memory while the other one streams: none (both
+// stream; a work unit is one output tile), or B (the whole B, N <= BN, loaded
+// once per CTA; a work unit is an M tile: the hidden layers of inference).
+// (Keeping an A tile resident across the output layer's N tiles was
+// measured: no faster per tile, its work units balance worse.)
+enum Resident : int { RES_NONE = 0, RES_B = 1 };
+
+// Words per row of the epilogue staging tile: 36 where a mode writes FP32
+// rows, 20 where it writes BF16 rows only (16-byte rows, conflict-free
+// quarter warps either way).
+template <int MODE>
+__host__ __device__ constexpr int stage_pitch() {
+  return (MODE == EP_HIDDEN_INFER || MODE == EP_DX) ? 20 : 36;
+}
+template <int BN, int RES>
+__host__ __device__ constexpr int res_box() { return RES == RES_B ? BN * BK * 2 : 0; }
+template <int BN, int RES>
+__host__ __device__ constexpr int ring_box() { return RES == RES_B ? A_STAGE : A_STAGE + BN * BK * 2; }
+template <int BN, int MODE, int RES>
+__host__ __device__ constexpr int stages() {
+  // as many ring stages (at most 4) as fit beside the resident operand and
+  // the staging tiles in 227 KB
+  return (232448 - 1024 - 512 - (RES == RES_NONE ? 0 : (K_MAX / BK) * res_box<BN, RES>()) -
+          EPI_WARPS * 32 * stage_pitch<MODE>() * 4) / ring_box<BN, RES>() >= 4
+             ? 4
+             : (232448 - 1024 - 512 - (RES == RES_NONE ? 0 : (K_MAX / BK) * res_box<BN, RES>()) -
+                EPI_WARPS * 32 * stage_pitch<MODE>() * 4) / ring_box<BN, RES>();
+}
 
 struct GemmArgs {
   int M, N, K;              // C[M, N] = A[M, K] . B[N, K]^T, multiples of 128 / BN / 64
@@ -160,25 +188,36 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// SiLU and its derivative with the fast exponential and division: the
-// results are rounded to BF16 right after.
-__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+// SiLU and its derivative through the logistic function written with the
+// hardware's approximate hyperbolic tangent, sigma(z) = (1 + tanh(z / 2)) / 2:
+// one special-function instruction per element (the epilogue of a hidden
+// layer is bound by them; an exponential and a division take two).  Its
+// relative error (about 2^-11) is below the BF16 rounding that follows.
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float silu_f(float z) {
+  const float h = 0.5f * z;
+  return fmaf(h, tanh_approx(h), h);
+}
 __device__ __forceinline__ float dsilu_f(float z) {
-  const float s = __frcp_rn(1.f + __expf(-z));
+  const float s = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
   return s * (1.f + z * (1.f - s));
 }
 
 // Row-major store of a warp's 32-row block (thread = row, W 32-bit words
-// per row) through the warp's staging tile: the block is written in the
-// thread-per-row layout and read back so that each lane carries VB
-// consecutive bytes of one row and each store instruction writes whole rows
-// (full sectors), rows from `row0` of `base` with pitch `pitch` bytes.
-constexpr int STAGE_PITCH = 36;   // words per staging row (16-byte rows, conflict-free quarter warps)
-
-template <int W, int VB>
+// per row) through the warp's staging tile (P words per row): the block is
+// written in the thread-per-row layout and read back so that each lane
+// carries VB consecutive bytes of one row and each store instruction writes
+// whole rows (full sectors), rows from `row0` of `base` with pitch `pitch`
+// bytes.
+template <int W, int VB, int P>
 __device__ __forceinline__ void store_rows(uint32_t* buf, const uint32_t (&w)[W], int lane, char* base, int row0,
                                            size_t pitch, int rows, int wlim = W) {
-  static_assert(W % 4 == 0 && (VB == 16 || VB == 8 || VB == 4), "staged row store shape");
+  static_assert(W % 4 == 0 && W <= P && P % 4 == 0 && (VB == 16 || VB == 8 || VB == 4), "staged row store shape");
+  constexpr int STAGE_PITCH = P;
 #pragma unroll
   for (int q = 0; q < W; q += 4)
     *reinterpret_cast<uint4*>(buf + lane * STAGE_PITCH + q) = make_uint4(w[q], w[q + 1], w[q + 2], w[q + 3]);
@@ -222,9 +261,7 @@ __device__ __forceinline__ void epilogue_chunk(const GemmArgs& a, uint32_t* buf,
   const bool row_ok = lane < rows;
   // bias, four columns at a time (the same address in every lane)
   const float4* bp = reinterpret_cast<const float4*>(a.bias + n);
-  switch (MODE) {
-    case EP_HIDDEN:
-    case EP_HIDDEN_INFER: {
+  if constexpr (MODE == EP_HIDDEN || MODE == EP_HIDDEN_INFER) {
       uint32_t zw[32], hw[16];
 #pragma unroll
       for (int q = 0; q < 32; q += 4) {
@@ -232,22 +269,22 @@ __device__ __forceinline__ void epilogue_chunk(const GemmArgs& a, uint32_t* buf,
         zw[q] = __float_as_uint(v[q] + b4.x); zw[q + 1] = __float_as_uint(v[q + 1] + b4.y);
         zw[q + 2] = __float_as_uint(v[q + 2] + b4.z); zw[q + 3] = __float_as_uint(v[q + 3] + b4.w);
       }
-      if (MODE == EP_HIDDEN)
-        store_rows<32, 16>(buf, zw, lane, reinterpret_cast<char*>(a.z + n), row0, (size_t)a.ldz * 4, rows);
+      if constexpr (MODE == EP_HIDDEN)
+        store_rows<32, 16, stage_pitch<MODE>()>(buf, zw, lane, reinterpret_cast<char*>(a.z + n), row0,
+                                                (size_t)a.ldz * 4, rows);
 #pragma unroll
       for (int q = 0; q < 16; ++q)
         hw[q] = pack_bf16(silu_f(__uint_as_float(zw[2 * q])), silu_f(__uint_as_float(zw[2 * q + 1])));
-      if (MODE == EP_HIDDEN) {
+      if constexpr (MODE == EP_HIDDEN) {
         if (row_ok) {
           const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(hw);
 #pragma unroll
           for (int q = 0; q < 32; ++q) a.out_t[(size_t)(n + q) * a.ldt + m] = h[q];
         }
       }
-      store_rows<16, 16>(buf, hw, lane, reinterpret_cast<char*>(a.out_bf16 + n), row0, (size_t)a.ldb * 2, rows);
-      break;
-    }
-    case EP_OUT: {
+      store_rows<16, 16, stage_pitch<MODE>()>(buf, hw, lane, reinterpret_cast<char*>(a.out_bf16 + n), row0,
+                                              (size_t)a.ldb * 2, rows);
+  } else if constexpr (MODE == EP_OUT) {
       uint32_t yw[32];
 #pragma unroll
       for (int q = 0; q < 32; q += 4) {
@@ -258,19 +295,17 @@ __device__ __forceinline__ void epilogue_chunk(const GemmArgs& a, uint32_t* buf,
       // y rows have the caller's pitch: pieces as wide as its alignment allows
       const int wlim = a.n_valid - n < 32 ? a.n_valid - n : 32;
       char* yb = reinterpret_cast<char*>(a.out_f32 + n);
-      if ((a.ldo & 3) == 0) store_rows<32, 16>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
-      else if ((a.ldo & 1) == 0) store_rows<32, 8>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
-      else store_rows<32, 4>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
-      break;
-    }
-    case EP_DW: {
+      constexpr int P = stage_pitch<MODE>();
+      if ((a.ldo & 3) == 0) store_rows<32, 16, P>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
+      else if ((a.ldo & 1) == 0) store_rows<32, 8, P>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
+      else store_rows<32, 4, P>(buf, yw, lane, yb, row0, (size_t)a.ldo * 4, rows, wlim);
+  } else if constexpr (MODE == EP_DW) {
       uint32_t gw[32];
 #pragma unroll
       for (int q = 0; q < 32; ++q) gw[q] = __float_as_uint(v[q]);
-      store_rows<32, 16>(buf, gw, lane, reinterpret_cast<char*>(a.out_f32 + n), row0, (size_t)a.ldo * 4, rows);
-      break;
-    }
-    case EP_DX: {
+      store_rows<32, 16, stage_pitch<MODE>()>(buf, gw, lane, reinterpret_cast<char*>(a.out_f32 + n), row0,
+                                              (size_t)a.ldo * 4, rows);
+  } else if constexpr (MODE == EP_DX) {
       uint32_t gw[16];
       if (row_ok) {
         const float4* zp = reinterpret_cast<const float4*>(a.z + (size_t)m * a.ldz + n);
@@ -287,45 +322,57 @@ __device__ __forceinline__ void epilogue_chunk(const GemmArgs& a, uint32_t* buf,
 #pragma unroll
         for (int q = 0; q < 16; ++q) gw[q] = 0u;
       }
-      store_rows<16, 16>(buf, gw, lane, reinterpret_cast<char*>(a.out_bf16 + n), row0, (size_t)a.ldb * 2, rows);
-      break;
-    }
+      store_rows<16, 16, stage_pitch<MODE>()>(buf, gw, lane, reinterpret_cast<char*>(a.out_bf16 + n), row0,
+                                              (size_t)a.ldb * 2, rows);
   }
 }
 
 // ------------------------------------------------------------ GEMM ----
-template <int BN>
+template <int BN, int MODE, int RES>
 __host__ __device__ constexpr size_t gemm_smem_bytes() {
-  return 1024 + (size_t)stages<BN>() * (A_STAGE + BN * BK * 2) + (size_t)EPI_WARPS * 32 * STAGE_PITCH * 4 +
-         (2 * stages<BN>() + 5) * 8 + 16;
+  return 1024 + (RES == RES_NONE ? 0 : (size_t)(K_MAX / BK) * res_box<BN, RES>()) +
+         (size_t)stages<BN, MODE, RES>() * ring_box<BN, RES>() + (size_t)EPI_WARPS * 32 * stage_pitch<MODE>() * 4 +
+         (2 * stages<BN, MODE, RES>() + 7) * 8 + 16;
 }
 
-template <int BN, int MODE>
+// Work unit u of the CTA: its M tile and its N tiles [nt0, nt1).
+template <int RES>
+__device__ __forceinline__ void unit_tiles(int u, int tiles_n, int& mt, int& nt0, int& nt1) {
+  if (RES == RES_NONE) { mt = u / tiles_n; nt0 = u % tiles_n; nt1 = nt0 + 1; }
+  else { mt = u; nt0 = 0; nt1 = 1; }
+}
+
+template <int BN, int MODE, int RES>
 __global__ void __launch_bounds__(THREADS, 1)
     k_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmArgs a) {
-  constexpr int S = stages<BN>();
-  constexpr int B_STAGE = BN * BK * 2;
-  static_assert(gemm_smem_bytes<BN>() <= 232448, "shared memory of one CTA");
+  constexpr int S = stages<BN, MODE, RES>();
+  constexpr int RBOX = res_box<BN, RES>(), SBOX = ring_box<BN, RES>();
+  constexpr int P = stage_pitch<MODE>();
+  static_assert(S >= 2 && gemm_smem_bytes<BN, MODE, RES>() <= 232448, "shared memory of one CTA");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + S * A_STAGE;
-  uint32_t* stage_all = reinterpret_cast<uint32_t*>(sB + S * B_STAGE);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(stage_all + EPI_WARPS * 32 * STAGE_PITCH);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 5);
+  uint8_t* sRes = smem;                                                         // resident operand, K / 64 boxes
+  uint8_t* sRing = sRes + (RES == RES_NONE ? 0 : (K_MAX / BK) * RBOX);           // stage ring
+  uint32_t* stage_all = reinterpret_cast<uint32_t*>(sRing + S * SBOX);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stage_all + EPI_WARPS * 32 * P);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 7);
   __shared__ volatile int bail;        // a wait of this CTA expired
-  __shared__ int issued;               // stage loads the producer issued
+  __shared__ int issued, res_issued;   // stage loads / resident loads the producer issued
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles_n = a.N / BN, tiles = ((a.M + BM - 1) / BM) * tiles_n;
+  const int tiles_n = a.N / BN, tiles_m = (a.M + BM - 1) / BM;
+  const int units = RES == RES_NONE ? tiles_m * tiles_n : tiles_m;
   const int nk = a.K / BK;
   const int mlim = (MODE == EP_OUT || MODE == EP_DW) ? a.m_valid : a.M;
-  // barriers: full[S], empty[S] (stage ring), accf[2], acce[2] (accumulators), done
+  // barriers: full[S], empty[S] (ring), accf[2], acce[2] (accumulators),
+  // done, resf (resident operand), rese (unused with B resident)
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), accf0 = smem_u32(bars + 2 * S),
-                 acce0 = smem_u32(bars + 2 * S + 2), done = smem_u32(bars + 2 * S + 4);
+                 acce0 = smem_u32(bars + 2 * S + 2), done = smem_u32(bars + 2 * S + 4),
+                 resf = smem_u32(bars + 2 * S + 5), rese = smem_u32(bars + 2 * S + 6);
 
   if (threadIdx.x == 0) {
     bail = 0;
     issued = 0;
+    res_issued = 0;
     for (int s = 0; s < S; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
@@ -335,6 +382,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(acce0 + 8 * b, EPI_WARPS);
     }
     mbar_init(done, 1);
+    mbar_init(resf, 1);
+    mbar_init(rese, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -352,16 +401,26 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 0) {
     if (lane == 0) {
       // TMA producer
-      int g = 0;
-      for (int t = blockIdx.x; t < tiles && !bail; t += gridDim.x) {
-        const int m0 = (t / tiles_n) * BM, n0 = (t % tiles_n) * BN;
-        for (int k = 0; k < nk; ++k) {
-          const int s = g % S;
-          if (g >= S && !mbar_wait(empty0 + 8 * s, ((uint32_t)(g / S) & 1u) ^ 1u, a.err)) { bail = 1; break; }
-          mbar_expect_tx(full0 + 8 * s, A_STAGE + B_STAGE);
-          tma_load_2d(smem_u32(sA + s * A_STAGE), &ta, full0 + 8 * s, k * BK, m0);
-          tma_load_2d(smem_u32(sB + s * B_STAGE), &tb, full0 + 8 * s, k * BK, n0);
-          ++g;
+      int g = 0, v = 0;
+      for (int u = blockIdx.x; u < units && !bail; u += gridDim.x, ++v) {
+        int mt, nt0, nt1;
+        unit_tiles<RES>(u, tiles_n, mt, nt0, nt1);
+        if (RES == RES_B && v == 0) {
+          // the whole B, once per CTA
+          mbar_expect_tx(resf, (uint32_t)(nk * RBOX));
+          for (int k = 0; k < nk; ++k) tma_load_2d(smem_u32(sRes + k * RBOX), &tb, resf, k * BK, 0);
+          res_issued = 1;
+        }
+        for (int nt = nt0; nt < nt1 && !bail; ++nt) {
+          for (int k = 0; k < nk; ++k) {
+            const int s = g % S;
+            if (g >= S && !mbar_wait(empty0 + 8 * s, ((uint32_t)(g / S) & 1u) ^ 1u, a.err)) { bail = 1; break; }
+            mbar_expect_tx(full0 + 8 * s, SBOX);
+            uint8_t* st = sRing + s * SBOX;
+            tma_load_2d(smem_u32(st), &ta, full0 + 8 * s, k * BK, mt * BM);
+            if (RES == RES_NONE) tma_load_2d(smem_u32(st + A_STAGE), &tb, full0 + 8 * s, k * BK, nt * BN);
+            ++g;
+          }
         }
       }
       issued = g;
@@ -370,25 +429,34 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       // MMA issuer: tile j accumulates into buffer j & 1
       constexpr uint32_t idesc = f16_idesc(BM, BN);
-      int g = 0, j = 0;
-      for (int t = blockIdx.x; t < tiles && !bail; t += gridDim.x, ++j) {
-        const int b = j & 1;
-        if (j >= 2 && !mbar_wait(acce0 + 8 * b, ((uint32_t)(j >> 1) & 1u) ^ 1u, a.err)) { bail = 1; break; }
-        tmem_fence_after();
-        const uint32_t acc = tmem + (uint32_t)(b * BN);
-        bool ok = true;
-        for (int k = 0; k < nk; ++k, ++g) {
-          const int s = g % S;
-          if (!mbar_wait(full0 + 8 * s, (uint32_t)(g / S) & 1u, a.err)) { ok = false; bail = 1; break; }
+      int g = 0, j = 0, v = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < units && ok && !bail; u += gridDim.x, ++v) {
+        int mt, nt0, nt1;
+        unit_tiles<RES>(u, tiles_n, mt, nt0, nt1);
+        if (RES == RES_B && v == 0) {
+          if (!mbar_wait(resf, 0u, a.err)) { ok = false; bail = 1; break; }
           tmem_fence_after();
-          const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
-#pragma unroll
-          for (int kk = 0; kk < BK / 16; ++kk)
-            mma_bf16(acc, sw128_desc(a0 + 32 * kk), sw128_desc(b0 + 32 * kk), idesc, (k > 0 || kk > 0) ? 1u : 0u);
-          mma_commit(empty0 + 8 * s);
         }
-        if (!ok) break;
-        mma_commit(accf0 + 8 * b);   // arrives when the tile's MMAs have completed
+        for (int nt = nt0; nt < nt1 && ok; ++nt, ++j) {
+          const int b = j & 1;
+          if (j >= 2 && !mbar_wait(acce0 + 8 * b, ((uint32_t)(j >> 1) & 1u) ^ 1u, a.err)) { ok = false; bail = 1; break; }
+          tmem_fence_after();
+          const uint32_t acc = tmem + (uint32_t)(b * BN);
+          for (int k = 0; k < nk; ++k, ++g) {
+            const int s = g % S;
+            if (!mbar_wait(full0 + 8 * s, (uint32_t)(g / S) & 1u, a.err)) { ok = false; bail = 1; break; }
+            tmem_fence_after();
+            const uint32_t st = smem_u32(sRing + s * SBOX);
+            const uint32_t a0 = st, b0 = RES == RES_NONE ? st + A_STAGE : smem_u32(sRes + k * RBOX);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk)
+              mma_bf16(acc, sw128_desc(a0 + 32 * kk), sw128_desc(b0 + 32 * kk), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+            mma_commit(empty0 + 8 * s);
+          }
+          if (!ok) break;
+          mma_commit(accf0 + 8 * b);   // arrives when the tile's MMAs have completed
+        }
       }
       mma_commit(done);   // arrives when every MMA issued above has completed
     }
@@ -398,32 +466,39 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int ew = warp - 2;
     const int quarter = warp & 3;
     constexpr int GROUPS = EPI_WARPS / 4;
+    uint32_t* buf = stage_all + ew * 32 * P;
     int j = 0;
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++j) {
-      const int b = j & 1;
-      if (!mbar_wait(accf0 + 8 * b, (uint32_t)(j >> 1) & 1u, a.err)) { bail = 1; break; }
-      tmem_fence_after();
-      const int row0 = (t / tiles_n) * BM + quarter * 32, n0 = (t % tiles_n) * BN;
-      const int rows = mlim - row0 < 32 ? mlim - row0 : 32;
-      uint32_t* buf = stage_all + ew * 32 * STAGE_PITCH;
-      for (int c0 = (ew >> 2) * 32; c0 < BN; c0 += 32 * GROUPS) {
-        float v[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN + c0), v);
-        epilogue_chunk<MODE>(a, buf, v, row0, n0 + c0, rows, lane);
+    bool ok = true;
+    for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+      int mt, nt0, nt1;
+      unit_tiles<RES>(u, tiles_n, mt, nt0, nt1);
+      for (int nt = nt0; nt < nt1; ++nt, ++j) {
+        const int b = j & 1;
+        if (!mbar_wait(accf0 + 8 * b, (uint32_t)(j >> 1) & 1u, a.err)) { ok = false; bail = 1; break; }
+        tmem_fence_after();
+        const int row0 = mt * BM + quarter * 32, n0 = nt * BN;
+        const int rows = mlim - row0 < 32 ? mlim - row0 : 32;
+        for (int c0 = (ew >> 2) * 32; c0 < BN; c0 += 32 * GROUPS) {
+          float v[32];
+          tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN + c0), v);
+          epilogue_chunk<MODE>(a, buf, v, row0, n0 + c0, rows, lane);
+        }
+        tmem_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce0 + 8 * b);
       }
-      tmem_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acce0 + 8 * b);
     }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    // every MMA has completed, and so has every stage load that was issued
-    // (the most recent phase of each stage; on the normal path all were
-    // consumed), before the tensor memory is freed and the CTA exits
+    // every MMA has completed, and so has every load that was issued (the
+    // most recent phase of each stage and of the resident operand; on the
+    // normal path all were consumed), before the tensor memory is freed and
+    // the CTA exits
     mbar_wait(done, 0, a.err);
     const int g1 = issued;
     for (int g = g1 - S < 0 ? 0 : g1 - S; g < g1; ++g) mbar_wait(full0 + 8 * (g % S), (uint32_t)(g / S) & 1u, a.err);
+    if (res_issued > 0) mbar_wait(resf, 0u, a.err);
   }
   tmem_fence_before();
   __syncthreads();
@@ -590,38 +665,51 @@ int status_of(mpcmd_mlp* m) {
 }
 
 // One persistent CTA per SM (at most one per tile).
-template <int BN, int MODE>
+template <int BN, int MODE, int RES>
 void launch_one(mpcmd_mlp* m, int grid, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g) {
-  k_gemm<BN, MODE><<<grid, THREADS, gemm_smem_bytes<BN>(), m->st>>>(ta, tb, g);
+  k_gemm<BN, MODE, RES><<<grid, THREADS, gemm_smem_bytes<BN, MODE, RES>(), m->st>>>(ta, tb, g);
 }
 
 template <int BN>
-void launch_bn(mpcmd_mlp* m, int grid, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g) {
+void launch_bn(mpcmd_mlp* m, int grid, int res, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g) {
   switch (g.mode) {
-    case EP_HIDDEN: launch_one<BN, EP_HIDDEN>(m, grid, ta, tb, g); break;
-    case EP_HIDDEN_INFER: launch_one<BN, EP_HIDDEN_INFER>(m, grid, ta, tb, g); break;
-    case EP_OUT: launch_one<BN, EP_OUT>(m, grid, ta, tb, g); break;
-    case EP_DX: launch_one<BN, EP_DX>(m, grid, ta, tb, g); break;
-    default: launch_one<BN, EP_DW>(m, grid, ta, tb, g); break;
+    case EP_HIDDEN: launch_one<BN, EP_HIDDEN, RES_NONE>(m, grid, ta, tb, g); break;
+    case EP_HIDDEN_INFER:
+      if (res == RES_B) launch_one<BN, EP_HIDDEN_INFER, RES_B>(m, grid, ta, tb, g);
+      else launch_one<BN, EP_HIDDEN_INFER, RES_NONE>(m, grid, ta, tb, g);
+      break;
+    case EP_OUT: launch_one<BN, EP_OUT, RES_NONE>(m, grid, ta, tb, g); break;
+    case EP_DX: launch_one<BN, EP_DX, RES_NONE>(m, grid, ta, tb, g); break;
+    default: launch_one<BN, EP_DW, RES_NONE>(m, grid, ta, tb, g); break;
   }
+}
+
+template <int BN, int MODE, int RES>
+bool allow_one() {
+  return cudaFuncSetAttribute(k_gemm<BN, MODE, RES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)gemm_smem_bytes<BN, MODE, RES>()) == cudaSuccess;
 }
 
 template <int BN>
 bool allow_smem() {
-  const int b = (int)gemm_smem_bytes<BN>();
-  return cudaFuncSetAttribute(k_gemm<BN, EP_HIDDEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
-         cudaFuncSetAttribute(k_gemm<BN, EP_HIDDEN_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
-         cudaFuncSetAttribute(k_gemm<BN, EP_OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
-         cudaFuncSetAttribute(k_gemm<BN, EP_DX>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
-         cudaFuncSetAttribute(k_gemm<BN, EP_DW>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess;
+  return allow_one<BN, EP_HIDDEN, RES_NONE>() && allow_one<BN, EP_HIDDEN_INFER, RES_NONE>() &&
+         allow_one<BN, EP_HIDDEN_INFER, RES_B>() && allow_one<BN, EP_OUT, RES_NONE>() &&
+         allow_one<BN, EP_DX, RES_NONE>() && allow_one<BN, EP_DW, RES_NONE>();
 }
 
+// One persistent CTA per SM (at most one per work unit).  The hidden layers
+// of inference keep their weights resident (the whole N fits one tile).
 int launch_gemm(mpcmd_mlp* m, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g, int BN) {
-  const int tiles = ((g.M + BM - 1) / BM) * (g.N / BN);
-  const int grid = tiles < m->sms ? tiles : m->sms;
-  if (BN == 256) launch_bn<256>(m, grid, ta, tb, g);
-  else if (BN == 128) launch_bn<128>(m, grid, ta, tb, g);
-  else launch_bn<64>(m, grid, ta, tb, g);
+  const int tiles_n = g.N / BN, tiles_m = (g.M + BM - 1) / BM;
+  int res = RES_NONE, units = tiles_m * tiles_n;
+  if (g.mode == EP_HIDDEN_INFER && tiles_n == 1 && g.K <= K_MAX) {
+    res = RES_B;
+    units = tiles_m;
+  }
+  const int grid = units < m->sms ? units : m->sms;
+  if (BN == 256) launch_bn<256>(m, grid, res, ta, tb, g);
+  else if (BN == 128) launch_bn<128>(m, grid, res, ta, tb, g);
+  else launch_bn<64>(m, grid, res, ta, tb, g);
   return cudaPeekAtLastError() == cudaSuccess ? MPCMD_OK : MPCMD_ERR_CUDA;
 }
 
