@@ -8,22 +8,23 @@
 // persistent kernel, k_gemm, with one CTA per SM walking its share of the
 // 128 x BN output tiles.  Warp roles: one thread streams the A and B tiles
 // into a ring of shared-memory stages with TMA (cp.async.bulk.tensor,
-// 128-byte swizzle, mbarriers); one thread issues tcgen05.mma (kind::f16,
-// BF16 operands, FP32 accumulator in tensor memory) and releases each stage
-// with tcgen05.commit; eight epilogue warps read the accumulator back with
-// tcgen05.ld (a warp reaches the 32 TMEM lanes of its quarter; two warps
-// share a quarter, one column half each) and apply the fused epilogue: bias
-// + SiLU with the pre-activation kept for the backward pass (forward
-// hidden), bias (output), SiLU' of the kept pre-activation (input
-// gradient), or the FP32 weight gradient.  Two accumulators in tensor
-// memory let the epilogue of one tile overlap the loads and MMAs of the
-// next.  Row-major outputs go through a per-warp 32 x 32 staging tile in
-// shared memory so that every store writes a row's contiguous columns; the
-// forms that the next GEMM needs transposed are also written from the
-// thread-per-row layout, so that every operand stays K-major.  Every
-// mbarrier wait is bounded (two seconds of globaltimer): on expiry the
-// kernel raises an error flag, skips its remaining work, waits for its
-// copies and MMAs in flight and still frees its tensor memory.
+// 128-byte swizzle, mbarriers), or keeps B resident when all of it fits one
+// tile (the hidden layers of inference); one thread issues tcgen05.mma
+// (kind::f16, BF16 operands, FP32 accumulator in tensor memory) and releases
+// each stage with tcgen05.commit; sixteen epilogue warps read the
+// accumulator back with tcgen05.ld (a warp reaches the 32 TMEM lanes of its
+// quarter; the four warps of a quarter take its 32-column chunks in turn)
+// and apply the fused epilogue: bias + SiLU with the pre-activation kept for
+// the backward pass (forward hidden), bias + SiLU (inference), bias
+// (output), SiLU' of the kept pre-activation (input gradient), or the FP32
+// weight gradient.  Two accumulators in tensor memory let the epilogue of
+// one tile overlap the loads and MMAs of the next.  Row-major outputs go
+// through a per-warp 32-row staging tile in shared memory so that every
+// store writes whole rows; the forms that the next GEMM needs transposed are
+// written from the thread-per-row layout, so that every operand stays
+// K-major.  Every mbarrier wait is bounded (two seconds of globaltimer): on
+// expiry the kernel raises an error flag, skips its remaining work, waits
+// for its copies and MMAs in flight and still frees its tensor memory.
 //
 // Weights are kept in FP32 (master copy for Adam) and in BF16 twice: [N, K]
 // for the forward GEMM and [K, N] for the input-gradient GEMM.
@@ -332,7 +333,7 @@ template <int BN, int MODE, int RES>
 __host__ __device__ constexpr size_t gemm_smem_bytes() {
   return 1024 + (RES == RES_NONE ? 0 : (size_t)(K_MAX / BK) * res_box<BN, RES>()) +
          (size_t)stages<BN, MODE, RES>() * ring_box<BN, RES>() + (size_t)EPI_WARPS * 32 * stage_pitch<MODE>() * 4 +
-         (2 * stages<BN, MODE, RES>() + 7) * 8 + 16;
+         (2 * stages<BN, MODE, RES>() + 6) * 8 + 16;
 }
 
 // Work unit u of the CTA: its M tile and its N tiles [nt0, nt1).
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* sRing = sRes + (RES == RES_NONE ? 0 : (K_MAX / BK) * RBOX);           // stage ring
   uint32_t* stage_all = reinterpret_cast<uint32_t*>(sRing + S * SBOX);
   uint64_t* bars = reinterpret_cast<uint64_t*>(stage_all + EPI_WARPS * 32 * P);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 7);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 6);
   __shared__ volatile int bail;        // a wait of this CTA expired
   __shared__ int issued, res_issued;   // stage loads / resident loads the producer issued
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -364,10 +365,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int nk = a.K / BK;
   const int mlim = (MODE == EP_OUT || MODE == EP_DW) ? a.m_valid : a.M;
   // barriers: full[S], empty[S] (ring), accf[2], acce[2] (accumulators),
-  // done, resf (resident operand), rese (unused with B resident)
+  // done, resf (resident operand)
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), accf0 = smem_u32(bars + 2 * S),
                  acce0 = smem_u32(bars + 2 * S + 2), done = smem_u32(bars + 2 * S + 4),
-                 resf = smem_u32(bars + 2 * S + 5), rese = smem_u32(bars + 2 * S + 6);
+                 resf = smem_u32(bars + 2 * S + 5);
 
   if (threadIdx.x == 0) {
     bail = 0;
@@ -383,7 +384,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     mbar_init(done, 1);
     mbar_init(resf, 1);
-    mbar_init(rese, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
