@@ -2807,19 +2807,30 @@ __global__ void k_resort_bin(Dev<T> d, KParams<T> kp, int bits) {
       const int64_t i = base + 32 * u + lane;
       r[u] = i < kp.n ? d.skey[i] : 0u;
     }
+    // the groups of all four steps first, then their atomics (independent,
+    // all in flight at once), then the placements
+    unsigned peers[RESORT_UNROLL], am[RESORT_UNROLL];
+    uint32_t pos[RESORT_UNROLL];
 #pragma unroll
     for (int u = 0; u < RESORT_UNROLL; ++u) {
+      const bool act = base + 32 * u + lane < kp.n;
+      am[u] = __ballot_sync(0xffffffffu, act);
+      peers[u] = act ? __match_any_sync(am[u], r[u] >> bits) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < RESORT_UNROLL; ++u) {
+      pos[u] = 0u;
+      if (peers[u] && lane == __ffs(peers[u]) - 1) {
+        const uint32_t b = r[u] >> bits;
+        pos[u] = d.sstart[b] + atomicAdd(&d.sfill[b], (unsigned)__popc(peers[u]));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < RESORT_UNROLL; ++u) {
+      if (!peers[u]) continue;   // (lanes past the end; the others are exactly am[u])
+      const uint32_t p0 = __shfl_sync(am[u], pos[u], __ffs(peers[u]) - 1);
       const int64_t i = base + 32 * u + lane;
-      const bool act = i < kp.n;
-      const unsigned am = __ballot_sync(0xffffffffu, act);
-      if (!act) continue;
-      const uint32_t b = r[u] >> bits;
-      const unsigned peers = __match_any_sync(am, b);
-      const int lead = __ffs(peers) - 1;
-      uint32_t pos = 0u;
-      if (lane == lead) pos = d.sstart[b] + atomicAdd(&d.sfill[b], (unsigned)__popc(peers));
-      pos = __shfl_sync(am, pos, lead);
-      const uint32_t q = pos + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+      const uint32_t q = p0 + (uint32_t)__popc(peers[u] & ((1u << lane) - 1u));
       if (!chk(q < (uint32_t)kp.n, d.ctr, 132, q)) continue;
       d.sidx[q] = (uint32_t)i;
       d.watch[q] = r[u];
@@ -2939,10 +2950,12 @@ __global__ void __launch_bounds__(TPB, 3) k_resort_fine(Dev<T> d, KParams<T> kp,
 
 template <typename T>
 void Launch<T>::resort(Dev<T>& d, const KParams<T>& kp, int tc, int tc_full, cudaStream_t st) {
-  // bins of 2^bits ranks holding at most half the fine pass's capacity on average
+  // bins of 2^bits ranks holding at most 3/4 of the fine pass's capacity on
+  // average (larger bins spread the fine pass's fixed cost per bin over more
+  // particles; a bin's Poisson spread stays far below the capacity)
   const double per_cell = (double)kp.n / (double)kp.ncell;
   int bits = 0;
-  while (bits < RESORT_MAX_BITS && (double)(2 << bits) * per_cell <= 0.5 * RESORT_CAP) ++bits;
+  while (bits < RESORT_MAX_BITS && (double)(2 << bits) * per_cell <= 0.75 * RESORT_CAP) ++bits;
   const int nbins = (int)((kp.ncell + (1 << bits) - 1) >> bits);
   cudaMemsetAsync(d.scnt, 0, sizeof(uint32_t) * nbins, st);
   cudaMemsetAsync(d.sfill, 0, sizeof(uint32_t) * nbins, st);
