@@ -167,6 +167,22 @@ __device__ __forceinline__ void lj(const KParams<T>& kp, int t, T E, T dRsq, T d
   u = E * Ubrack;
 }
 
+// A cell's rotation record (centre-of-mass velocity, then axis) is six T at a
+// stride of six T, so each pair of values is aligned to twice its size: three
+// 8-byte (16-byte in FP64) loads read a record (six scalar loads made
+// k_rotate_main 10 % slower).
+template <typename T> struct Pair2;
+template <> struct Pair2<float> { using type = float2; };
+template <> struct Pair2<double> { using type = double2; };
+
+template <typename T>
+__device__ __forceinline__ void load_rot(const T* rot, uint32_t key, T* t) {
+  using V = typename Pair2<T>::type;
+  const V* r = reinterpret_cast<const V*>(rot + 6 * (size_t)key);
+  const V a = r[0], b = r[1], c = r[2];
+  t[0] = a.x; t[1] = a.y; t[2] = b.x; t[3] = b.y; t[4] = c.x; t[5] = c.y;
+}
+
 // Collision rotation of v - v_cm (mpc_rotation_mod.f95:205-228 Rodrigues form;
 // RMPC_SelkovDimer.f90:86-118 projection form).
 template <typename T>
@@ -1009,6 +1025,10 @@ void Launch<T>::finalize_rebuild(const Dev<T>& d, const KParams<T>& kp, const St
   LAUNCH_COUNT();
 }
 
+// k_force's sphere-sphere blocks: warps per sphere, spheres per block
+constexpr int SPH_WARPS = 4;
+constexpr int SPH_PER_BLOCK = (TPB / 32) / SPH_WARPS;
+
 // --------------------------------------------------------------- forces ----
 // Per shell particle and MD step (evolve_mod.f95:567-670 with
 // forces_mod.f95:6-140): LJ force against each sphere of its pair list in
@@ -1030,15 +1050,21 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
     }
   }
   if ((int)blockIdx.x >= a.g_force) {
-    // sphere-sphere forces: one warp per sphere s
-    int w = ((int)blockIdx.x - a.g_force) * (TPB / 32) + (threadIdx.x >> 5);
-    int lane = threadIdx.x & 31;
-    if (w >= kp.ns) return;
-    const int s = w, ks = s >> 1, is = s & 1;
+    // sphere-sphere forces: SPH_WARPS warps per sphere s, each over every
+    // SPH_WARPS-th group of 32 spheres, their sums added in warp order.  These
+    // blocks start only as the shell blocks retire, so their latency adds to
+    // the launch; a sphere's scan split four ways shortens it about fourfold.
+    __shared__ double s_part[TPB / 32][4];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int part = wib % SPH_WARPS;
+    const int sg = ((int)blockIdx.x - a.g_force) * SPH_PER_BLOCK + wib / SPH_WARPS;
+    const bool have = sg < kp.ns;   // (warp-uniform)
+    const int s = have ? sg : 0, ks = s >> 1, is = s & 1;
     const SphereRel<T> rs = d.srel[s];
     double fx = 0., fy = 0., fz = 0., pot = 0.;
     // (rotors have no motor-motor LJ: rotational_code/2d_array/evolve_mod.f95:515-531)
-    for (int t = lane; t < (kp.rotor ? 0 : kp.ns); t += 32) {
+    const int nt = (kp.rotor || !have) ? 0 : kp.ns;
+    for (int t = 32 * part + lane; t < nt; t += 32 * SPH_WARPS) {
       int kt = t >> 1, it = t & 1;
       if (kt == ks) continue;
       const SphereRel<T> rt = d.srel[t];
@@ -1073,8 +1099,12 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
       fz += __shfl_xor_sync(0xffffffffu, fz, o);
       pot += __shfl_xor_sync(0xffffffffu, pot, o);
     }
-    if (lane == 0) {
-      d.fmot[4 * s + 0] = fx; d.fmot[4 * s + 1] = fy; d.fmot[4 * s + 2] = fz; d.fmot[4 * s + 3] = pot;
+    if (lane == 0) { s_part[wib][0] = fx; s_part[wib][1] = fy; s_part[wib][2] = fz; s_part[wib][3] = pot; }
+    __syncthreads();
+    if (have && part == 0 && lane < 4) {
+      double v = 0.;
+      for (int q = 0; q < SPH_WARPS; ++q) v += s_part[wib + q][lane];
+      d.fmot[4 * s + lane] = v;
     }
     return;
   }
@@ -1239,7 +1269,7 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
 
 template <typename T>
 void Launch<T>::force(const Dev<T>& d, const KParams<T>& kp, const StepArgs& a, cudaStream_t st) {
-  int extra = (kp.ns + (TPB / 32) - 1) / (TPB / 32);
+  const int extra = (kp.ns + SPH_PER_BLOCK - 1) / SPH_PER_BLOCK;
   if (kp.owner_tags) k_force<T, true><<<a.g_force + extra, TPB, 0, st>>>(d, kp, a);
   else k_force<T, false><<<a.g_force + extra, TPB, 0, st>>>(d, kp, a);
   LAUNCH_COUNT();
@@ -1266,8 +1296,9 @@ __global__ void __launch_bounds__(TPB) k_shell_advance(Dev<T> d, KParams<T> kp, 
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)nin; j += stride) {
     T vx = d.sh.vx[j], vy = d.sh.vy[j], vz = d.sh.vz[j];
     if (rotate) {
-      uint32_t key = d.sh.skey[j];
-      rotate_v(kp, d.rot + 6 * (size_t)key, vx, vy, vz);
+      T r[6];
+      load_rot(d.rot, d.sh.skey[j], r);
+      rotate_v(kp, r, vx, vy, vz);
     }
     if (a.advance) {
       uint32_t cell = d.sh.cell[j];
@@ -2559,12 +2590,9 @@ __global__ void __launch_bounds__(TPB) k_rotate_main(Dev<T> d, KParams<T> kp, St
       if (r0) c0 = d.p.cell[i0];
       if (r1) c1 = d.p.cell[i1];
     }
-    T t0[6], t1[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-      t0[q] = r0 ? d.rot[6 * (size_t)k0 + q] : (T)0;
-      t1[q] = r1 ? d.rot[6 * (size_t)k1 + q] : (T)0;
-    }
+    T t0[6] = {}, t1[6] = {};
+    if (r0) load_rot(d.rot, k0, t0);
+    if (r1) load_rot(d.rot, k1, t1);
     T g0 = (T)3e38, g1 = (T)3e38;
     if (a.watch_build) {
       if (r0) g0 = __uint_as_float(d.gapf[gap_bin_of(kp.ngx, kp.ngy, c0)]);
