@@ -7,8 +7,14 @@ rotation angle 120 degrees, collision interval 0.5).
   N(0, kT/m) after 20 collision periods, and the kinetic temperature.
 * Momentum conservation: the total momentum (FP64 reduction of solvent and
   spheres) drifts by at most 1e-10 of sum |p_i| over 100 collision periods in
-  the FP64 build; the FP32 build's drift is the random walk of the half-ulp
-  roundings of its FP32 velocity updates and is bounded at 2e-9 of sum |p_i|.
+  the FP64 build.  The FP32 build's drift is a random walk: every collision
+  rounds each stored velocity (half an ulp, about 1e-8 at v ~ 0.4) and each
+  cell's FP32 sum (its mean is off by about sqrt(n) ulps, and the rotation
+  turns that error), which over 100 periods of 270,000 particles in 27,000
+  cells gives a standard deviation near 5e-10 of sum |p_i| per component;
+  the cell sums are FP32 atomics in no fixed order, so the walk differs
+  from run to run (the worst of 10 checkpoints x 3 components was seen
+  between 1e-9 and 2.2e-9).  The bound is 1e-8.
 * Solvent self-diffusion against the FP64 reference algorithm (the oracle) on
   independent seeds, within two standard errors of the difference (standard
   errors from the spread of the replicas), and both within 10 % of the
@@ -65,7 +71,7 @@ def _abs_momentum(st, cfg):
     return float(p.sum() + (np.abs(st["dvel"]).sum(axis=1) * sm).sum())
 
 
-@pytest.mark.parametrize("prec,bound", [(64, 1e-10), (32, 2e-9)])
+@pytest.mark.parametrize("prec,bound", [(64, 1e-10), (32, 1e-8)])
 def test_momentum_conservation(prec, bound):
     cfg, e = _engine(prec)
     p0 = e.observables()["momentum"]
