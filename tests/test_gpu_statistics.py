@@ -26,6 +26,15 @@ rotation angle 120 degrees, collision interval 0.5).
   is a bias check, not a 2-SE target.
 * Dimer propulsion speed (the axial velocity of Output_SelkovDimer.f90:
   168-172) of FP32 and FP64 ensembles, within two standard errors.
+
+The two-ensemble comparisons state their result in standard errors of the
+difference (z in the assertion message).  The GPU runs are not
+bit-reproducible (the FP32 and FP64 cell sums and sphere sums are atomics in
+no fixed order, and the MD amplifies the last-bit differences), so every run
+of these tests is a fresh draw: with 6 + 6 and 8 + 8 replicas a correct build
+exceeds 2 SE in about 7 % of runs (Student t, 10 and 14 degrees of freedom).
+The assertions therefore take 3 SE (about 1 % of correct runs); every run
+recorded before this bound was set passed at 2 SE.
 """
 import math
 import os
@@ -40,6 +49,7 @@ from oracle.oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 THREADS = os.cpu_count() or 1
+Z_BOUND = 3.0   # standard errors of the difference (see the module docstring)
 
 
 def _engine(prec, seed=1):
@@ -120,7 +130,8 @@ def test_solvent_diffusion_fp32_against_reference_algorithm():
         d64.append(_msd_diffusion(o.get_state, lambda: o.run(S), c64, periods, t1))
     m32, m64 = np.mean(d32), np.mean(d64)
     se = math.sqrt(np.var(d32, ddof=1) / reps + np.var(d64, ddof=1) / reps)
-    assert abs(m32 - m64) <= 2.0 * se, (m32, m64, se)
+    z = abs(m32 - m64) / se
+    assert z <= Z_BOUND, (m32, m64, se, z)
     n = 10.0
     a = cfg["rot_angle"]
     formula = cfg["kT"] * cfg["mpc_dt"] / (2.0 * cfg["mass"][0]) * (
@@ -144,4 +155,5 @@ def test_dimer_propulsion_speed_fp32_against_fp64():
             e.close()
     a, b = np.array(speeds[32]), np.array(speeds[64])
     se = math.sqrt(a.var(ddof=1) / reps + b.var(ddof=1) / reps)
-    assert abs(a.mean() - b.mean()) <= 2.0 * se, (a.mean(), b.mean(), se)
+    z = abs(a.mean() - b.mean()) / se
+    assert z <= Z_BOUND, (a.mean(), b.mean(), se, z)
