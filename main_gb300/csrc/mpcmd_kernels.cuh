@@ -1064,6 +1064,7 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
     double fx = 0., fy = 0., fz = 0., pot = 0.;
     // (rotors have no motor-motor LJ: rotational_code/2d_array/evolve_mod.f95:515-531)
     const int nt = (kp.rotor || !have) ? 0 : kp.ns;
+    bool hit = false;   // a pair within its cutoff on this lane
     for (int t = 32 * part + lane; t < nt; t += 32 * SPH_WARPS) {
       int kt = t >> 1, it = t & 1;
       if (kt == ks) continue;
@@ -1083,6 +1084,7 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
       if (kp.geometry == 1) dz = min_image(dz, kp.Ld[2]);
       double dRsq = dx * dx + dy * dy + dz * dz;
       if (dRsq <= kp.mot_cut2[type]) {
+        hit = true;
         double IdRsq = 1.0 / dRsq;
         double IdR6 = IdRsq * IdRsq * IdRsq, IdR8 = IdR6 * IdRsq, IdR12 = IdR6 * IdR6, IdR14 = IdR12 * IdRsq;
         double Fb = 4.0 * (kp.mot_r12R12[type] * IdR14 - kp.mot_r6R6[type] * IdR8);
@@ -1093,11 +1095,16 @@ __global__ void __launch_bounds__(TPB, sizeof(T) == 4 ? 5 : 1) k_force(Dev<T> d,
         if (kt < ks) pot += kp.em * Ub;
       }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      fx += __shfl_xor_sync(0xffffffffu, fx, o);
-      fy += __shfl_xor_sync(0xffffffffu, fy, o);
-      fz += __shfl_xor_sync(0xffffffffu, fz, o);
-      pot += __shfl_xor_sync(0xffffffffu, pot, o);
+    // a warp none of whose pairs is within its cutoff (nearly every warp:
+    // the dimers are far apart) holds +0 everywhere and skips the FP64
+    // reduction, which at GB300's FP64 rate made the tail of every step
+    if (__any_sync(0xffffffffu, hit)) {
+      for (int o = 16; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        pot += __shfl_xor_sync(0xffffffffu, pot, o);
+      }
     }
     if (lane == 0) { s_part[wib][0] = fx; s_part[wib][1] = fy; s_part[wib][2] = fz; s_part[wib][3] = pot; }
     __syncthreads();
