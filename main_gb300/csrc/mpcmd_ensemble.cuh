@@ -774,6 +774,141 @@ __global__ void k_ens_dimer(EDev<T> d, int mode, int rattle_max) {
   if (iters) y.rattle_iters += iters;
 }
 
+// The FP32 build's dimer step with the three Cartesian components of a
+// replica's dimer on three lanes of a 4-lane group (the fourth lane holds
+// zeros and the replica's scalar work): the update of k_ens_dimer's fast
+// path, with every dot product summed over the group.  At GB300's FP64 rate
+// the per-replica chain of FP64 instructions sets the kernel's time, and the
+// split shortens it about threefold.  The group sums add the same terms in
+// the same order as the one-thread form ((x + y) + (z + 0)).
+template <typename T>
+__global__ void k_ens_dimer_split(EDev<T> d, int mode, int rattle_max) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = t >> 2, c = t & 3;
+  const unsigned gmask = 0xFu << (threadIdx.x & 28);   // this group's four lanes
+  const bool live = r < d.R;                            // the whole group agrees
+  Dyn<T>& y = d.dyn[live ? r : 0];
+  const Rep<T>& R = d.rep[live ? r : 0];
+  const KParams<T>& kp = R.kp;
+  const bool comp = c < 3;
+  const double L = kp.Ld[comp ? c : 0];
+  const double dt = kp.dtd, Mc = kp.mc, Mn = kp.mn, Dcn = kp.dcn;
+  const double hIMc = kp.hIMc, hIMn = kp.hIMn, IIM = kp.IIM;
+  double X1 = 0., X2 = 0., V1 = 0., V2 = 0., F1 = 0., F2 = 0., Q1 = 0., Q2 = 0.;
+  if (live && comp) {
+    X1 = y.dpos[c]; X2 = y.dpos[3 + c];
+    V1 = y.dvel[c]; V2 = y.dvel[3 + c];
+    F1 = y.dfrc[c]; F2 = y.dfrc[3 + c];
+    Q1 = y.dq[c]; Q2 = y.dq[3 + c];
+  }
+  unsigned long long iters = 0;
+  if (mode & M_VEL) {
+    if (live) {
+      // lane c takes the sphere sums c and 4 + c (lane 3: the potentials)
+      const double a1 = y.facc[c], a2 = y.facc[4 + c];
+      y.facc[c] = 0.; y.facc[4 + c] = 0.;
+      if (comp) { F1 = a1; F2 = a2; }
+      else y.pot = a1 + a2;
+    }
+    if (comp) { V1 = Q1 + hIMc * F1; V2 = Q2 + hIMn * F2; }
+    int acc = 0;
+    for (;;) {
+      const double dd = comp ? dmi(X1 - X2, L) : 0.;
+      const double Con2diff = 2.0 * group4_sum(gmask, (V1 - V2) * dd);
+      if (!live || fabs(Con2diff) < 1.e-8) break;
+      if (acc == rattle_max) { if (c == 0) atomicOr(&y.status, E_ERR_RATTLE); break; }
+      const double O2 = -(0.5 * (IIM * Con2diff) * kp.iD2);
+      V1 = V1 + O2 * dd * kp.iMc;
+      V2 = V2 - O2 * dd * kp.iMn;
+      acc++;
+    }
+    iters += acc;
+    if (live && comp) {
+      y.dvel[c] = V1; y.dvel[3 + c] = V2;
+      y.dfrc[c] = F1; y.dfrc[3 + c] = F2;
+    }
+    const unsigned step = d.g->cstep;
+    if (step % (unsigned)d.mpc_every == 0u) {
+      const double dd = comp ? dmi(X1 - X2, L) : 0.;
+      const double len = sqrt(group4_sum(gmask, dd * dd));
+      const double s = group4_sum(gmask, comp ? ((Mc * V1 + Mn * V2) / (Mn + Mc)) * (dd / len) : 0.);
+      if (live) {
+        const long long k = y.vdot_n;
+        if (d.hist > 0 && k < d.hist && comp) d.axes[((size_t)r * d.hist + k) * 3 + c] = (float)(dd / len);
+        __syncwarp(gmask);   // every lane has read vdot_n
+        if (c == 0) {
+          y.vdot_sum += s;
+          y.vdot_n = k + 1;
+          double u0, u1, u2, u3;
+          contract_pair(kp.seed, TAG_SHIFT, 0, 0, step, u0, u1);
+          contract_pair(kp.seed, TAG_SHIFT, 0, 1, step, u2, u3);
+          y.shift[0] = u0 - 0.5; y.shift[1] = u1 - 0.5; y.shift[2] = u2 - 0.5;
+          for (int q = 0; q < 3; ++q) y.shf[q] = (float)y.shift[q];
+        }
+      }
+    }
+  }
+  if (mode & M_POS) {
+    const unsigned step = d.g->cstep + 1u;
+    const double pr1 = X1, pr2 = X2;
+    const double dP = comp ? dmi(X1 - X2, L) : 0.;
+    if (comp) {
+      Q1 = V1 + hIMc * F1; Q2 = V2 + hIMn * F2;
+      X1 = X1 + dt * Q1; X2 = X2 + dt * Q2;
+    }
+    int acc = 0;
+    for (;;) {
+      const double dd = comp ? dmi(X1 - X2, L) : 0.;
+      const double Con1diff = group4_sum(gmask, dd * dd) - Dcn * Dcn;
+      if (!live || fabs(Con1diff) < 1.e-6) break;
+      if (acc == rattle_max) { if (c == 0) atomicOr(&y.status, E_ERR_RATTLE); break; }
+      const double den = group4_sum(gmask, dd * dP);
+      // a float reciprocal refined twice replaces the division (the
+      // iteration converges to the tolerance whatever G's last bits are)
+      double rr = (double)__frcp_rn((float)den);
+      rr = rr * (2.0 - den * rr);
+      rr = rr * (2.0 - den * rr);
+      const double G2 = 2.0 * (-(0.25 * Con1diff * IIM) * rr);
+      X1 = pr1 + Q1 * dt + G2 * dP * kp.iMc;
+      X2 = pr2 + Q2 * dt - G2 * dP * kp.iMn;
+      Q1 = Q1 + G2 * dP * kp.iMcdt;
+      Q2 = Q2 - G2 * dP * kp.iMndt;
+      acc++;
+    }
+    iters += acc;
+    if (live && comp) {
+      if (X1 >= L) X1 -= L; else if (X1 < 0.0) X1 += L;
+      if (X2 >= L) X2 -= L; else if (X2 < 0.0) X2 += L;
+      if (!(X1 >= 0.0 && X1 < L)) X1 = X1 - L * floor(X1 / L);
+      if (!(X2 >= 0.0 && X2 < L)) X2 = X2 - L * floor(X2 / L);
+      y.dpos[c] = X1; y.dpos[3 + c] = X2;
+      y.dq[c] = Q1; y.dq[3 + c] = Q2;
+      // the sphere positions as cell + offset (set_srel), one axis per lane
+      const double f1 = floor(X1), f2 = floor(X2);
+      SphereRel<T>& r1 = y.srel[0];
+      SphereRel<T>& r2 = y.srel[1];
+      if (c == 0) { r1.cx = (int)f1; r1.ox = (T)(X1 - f1); r2.cx = (int)f2; r2.ox = (T)(X2 - f2); }
+      else if (c == 1) { r1.cy = (int)f1; r1.oy = (T)(X1 - f1); r2.cy = (int)f2; r2.oy = (T)(X2 - f2); }
+      else { r1.cz = (int)f1; r1.oz = (T)(X1 - f1); r2.cz = (int)f2; r2.oz = (T)(X2 - f2); }
+    }
+    if (live && c == 3) {
+      // the rebuild decision (evolve_mod.f95:457-465)
+      const int tc = y.time_count + 1;
+      y.time_count = tc;
+      const double maxv = __longlong_as_double((long long)y.maxmsd);
+      const double thr = (double)kp.msd_thr;
+      const bool rb = maxv > thr || tc == y.time_penetrate || step % (unsigned)d.mpc_every == 0u;
+      y.maxmsd = 0ull;
+      if (rb) {
+        y.rebuild = 1;
+        y.n_shell = 0;
+        y.maxv2 = 0ull;
+      }
+    }
+  }
+  if (live && c == 0 && iters) y.rattle_iters += iters;
+}
+
 // ------------------------------------------------------------ collision ----
 // mpc_rotation_mod.f95:110-160 (shifted cell of every particle, collision
 // sums) fused with distribute_mod.f95:95-182 (per-species counts and first

@@ -269,7 +269,15 @@ struct Ensemble : EnsembleBase {
 
   // ---------------------------------------------------------- launches --
   void L_force(int mode) { k_ens_force<T><<<g_shell, sblock, 0, st>>>(d, mode); ++launches; }
-  void L_dimer(int mode) { k_ens_dimer<T><<<(R + 127) / 128, 128, 0, st>>>(d, mode, rattle_max); ++launches; }
+  void L_dimer(int mode) {
+    if (sizeof(T) == 4) {
+      // four lanes per replica, one 32-lane block per eight replicas (spread over the SMs)
+      k_ens_dimer_split<T><<<(4 * R + 31) / 32, 32, 0, st>>>(d, mode, rattle_max);
+    } else {
+      k_ens_dimer<T><<<(R + 127) / 128, 128, 0, st>>>(d, mode, rattle_max);
+    }
+    ++launches;
+  }
   void L_plan() { k_ens_plan<T><<<1, 1024, 0, st>>>(d); ++launches; }
   void L_rebuild(int mode) { k_ens_rebuild<T><<<g_part, block, 0, st>>>(d, mode); ++launches; }
   void L_finalize(int adv) { k_ens_finalize<T><<<1, 1024, 0, st>>>(d, sblock, adv); ++launches; }

@@ -146,3 +146,35 @@ def test_fp32_ensemble_conserves_and_autotunes(tmp_path):
     assert ns == 1 and counts.shape == (16, 16, 8) and counts.sum() > 0
     ens.close()
     ens2.close()
+
+
+def test_fp32_ensemble_follows_fp64_ensemble():
+    """The FP32 build (FP32 solvent, four lanes per replica in the dimer step)
+    follows the FP64 build from the same state: after 120 MD steps (two or
+    three collision steps) every replica's dimer positions and velocities
+    and the propulsion-speed samples and axes agree far inside what a wrong
+    component or a lost sphere sum would give (O(0.1) and larger)."""
+    reps = uneven_replicas(8, seed=11)
+    e64 = E.Ensemble(reps, precision=64)
+    e64.initial()
+    e32 = E.Ensemble(reps, precision=32)
+    for r in range(len(reps)):
+        e32.upload(r, e64.download(r))
+    for e in (e64, e32):
+        e.prepare()
+        e.reset_samples(history=4)
+        e.run(120)
+    for r in range(len(reps)):
+        a, b = e32.download(r), e64.download(r)
+        L = np.array([reps[r]["lx"], reps[r]["ly"], reps[r]["lz"]], float)
+        dp = a["dpos"] - b["dpos"]
+        dp -= L * np.round(dp / L)
+        assert np.abs(dp).max() <= 1e-3, (r, np.abs(dp).max())
+        assert np.abs(a["dvel"] - b["dvel"]).max() <= 1e-3, (r, np.abs(a["dvel"] - b["dvel"]).max())
+    m32, c32, ax32 = e32.samples()
+    m64, c64, ax64 = e64.samples()
+    assert np.array_equal(c32, c64) and np.all(c32 >= 2), (c32, c64)
+    assert np.abs(m32 - m64).max() <= 1e-3, np.abs(m32 - m64).max()
+    assert np.abs(ax32 - ax64).max() <= 1e-3
+    e32.close()
+    e64.close()
