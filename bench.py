@@ -546,7 +546,7 @@ def main_surrogate(args, ws, rk, lr):
     line = {"metric": METRIC, "value": sw["speedup_vs_single_context"], "unit": "x (sweep time plain / surrogate)",
             "n_gpus": ws, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * sw["screened_s"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (network), f32 (simulation)",
-            "data": "synthetic (seeded replicas simulated by this build)",
+            "data": "synthetic (seeded replicas simulated by the engine)",
             "config": {"workload": "learned surrogate: MLP 8 -> 4 x 256 SiLU -> 2 + 64 x 32, BF16 weights with FP32 "
                                    "accumulation, trained on %d batched-ensemble replicas (Adam, lr 1e-3, batch 256); "
                                    "%d-point sweep screened with plain-simulation fallback; %d collision periods per "

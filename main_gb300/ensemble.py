@@ -37,7 +37,8 @@ def _ptr(a, t):
 def replica(lx, ly=None, lz=None, density=10.0, n_solvent=None, seed=1, rc=4.0, rn=2.0, dcn=6.5,
             eps_c=(1.0, 1.0, 1.0, 1.0), eps_n=(1.0, 0.1, 1.0, 1.0), kT=1.0 / 6.0, k1=0.01,
             mass=(1.0, 1.0, 1.0, 1.0), mc=0.0, mn=0.0):
-    """Parameters of one replica (plain run of BASELINE configuration 0 by default)."""
+    """Parameters of one replica (by default the plain single-dimer run: sigma_C 4, sigma_N 2, bond 6.5,
+    density 10, kT 1/6, k1 0.01)."""
     ly = lx if ly is None else ly
     lz = lx if lz is None else lz
     n = int(round(density * lx * ly * lz)) if n_solvent is None else int(n_solvent)
