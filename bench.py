@@ -99,7 +99,7 @@ class Clocks:
         except Exception:
             self.proc = None
         # the timed region starts after the first sample: nvidia-smi's own
-        # start-up can hold the driver for a good part of a second, which
+        # start-up can hold the NVIDIA kernel driver for a good part of a second, which
         # would land inside a short timed region
         t0 = time.time()
         while self.proc is not None and time.time() - t0 < 10.0:
