@@ -152,8 +152,12 @@ def test_fp32_ensemble_follows_fp64_ensemble():
     """The FP32 build (FP32 solvent, four lanes per replica in the dimer step)
     follows the FP64 build from the same state: after 120 MD steps (two or
     three collision steps) every replica's dimer positions and velocities
-    and the propulsion-speed samples and axes agree far inside what a wrong
-    component or a lost sphere sum would give (O(0.1) and larger)."""
+    and the propulsion-speed samples and axes agree to 1e-2, far inside what
+    a wrong component or a lost sphere sum gives (O(0.1) and larger).  The
+    two builds drift apart by roundings (about 1e-5 here), and now and then
+    by a solvent particle that one build finds inside a cutoff and the other
+    just outside (a catalytic conversion one step apart), which can move a
+    dimer's velocity by about 1e-3; the bound leaves room for that."""
     reps = uneven_replicas(8, seed=11)
     e64 = E.Ensemble(reps, precision=64)
     e64.initial()
@@ -169,12 +173,12 @@ def test_fp32_ensemble_follows_fp64_ensemble():
         L = np.array([reps[r]["lx"], reps[r]["ly"], reps[r]["lz"]], float)
         dp = a["dpos"] - b["dpos"]
         dp -= L * np.round(dp / L)
-        assert np.abs(dp).max() <= 1e-3, (r, np.abs(dp).max())
-        assert np.abs(a["dvel"] - b["dvel"]).max() <= 1e-3, (r, np.abs(a["dvel"] - b["dvel"]).max())
+        assert np.abs(dp).max() <= 1e-2, (r, np.abs(dp).max())
+        assert np.abs(a["dvel"] - b["dvel"]).max() <= 1e-2, (r, np.abs(a["dvel"] - b["dvel"]).max())
     m32, c32, ax32 = e32.samples()
     m64, c64, ax64 = e64.samples()
     assert np.array_equal(c32, c64) and np.all(c32 >= 2), (c32, c64)
-    assert np.abs(m32 - m64).max() <= 1e-3, np.abs(m32 - m64).max()
-    assert np.abs(ax32 - ax64).max() <= 1e-3
+    assert np.abs(m32 - m64).max() <= 1e-2, np.abs(m32 - m64).max()
+    assert np.abs(ax32 - ax64).max() <= 1e-2
     e32.close()
     e64.close()
